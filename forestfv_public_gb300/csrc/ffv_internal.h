@@ -1,0 +1,57 @@
+// Internal declarations shared by the mesh builder (host C++) and the device code.
+#pragma once
+#include <stdint.h>
+
+#include "../../include/ffv.h"
+
+// Face kinds, 4 bits per face in a cell's info word (bits 4f..4f+3); level in bits 24..31.
+#define FFV_FK_SAME 0u     // one neighbour, same level (1:1 face)
+#define FFV_FK_COARSER 1u  // one neighbour, one level coarser (this cell is the fine side)
+#define FFV_FK_FINER 2u    // four neighbours, one level finer (subfaces)
+#define FFV_FK_BC 8u       // boundary: 8 | bc code
+
+static inline uint32_t ffv_face_kind(uint32_t info, int f) { return (info >> (4 * f)) & 15u; }
+static inline int ffv_info_level(uint32_t info) { return (int)(info >> 24); }
+
+// Hex corner k of a tree or child sits at (x, y, z) = (bit1(k), bit0(k), bit2(k)).  This is
+// the node order under which the reference's face normals (normalvector.c:23-29 applied to
+// the face-node table operatetp.c:64-69) point into the cell and its six-tet volume
+// (meshproperties.c:83-123) comes out negative -- the handedness its update
+// S = SN - DT/Vol*RHS needs to be upwind.  Child index = corner index (split.c:69-93).
+static inline int ffv_corner_x(int k) { return (k >> 1) & 1; }
+static inline int ffv_corner_y(int k) { return k & 1; }
+static inline int ffv_corner_z(int k) { return (k >> 2) & 1; }
+
+// Face f of a hex: its four nodes (operatetp.c:64-69, typ 0) and opposite face
+// (operatetp.c:268-279, fcopp).
+static const int ffv_face_nodes[6][4] = {{0, 1, 5, 4}, {3, 7, 5, 1}, {2, 6, 7, 3},
+                                         {2, 0, 4, 6}, {2, 3, 1, 0}, {6, 4, 5, 7}};
+static const int ffv_face_opp[6] = {2, 3, 0, 1, 5, 4};
+
+// Per-face frame for the Cartesian forest, derived by the builder from the reference's
+// normal/tangent formulas: component `axis` of the vector times `sign` (+1/-1).
+struct ffv_face_frame {
+  int8_t n_axis, n_sign, t1_axis, t1_sign, t2_axis, t2_sign;
+  int8_t side_axis, side_dir;  // domain axis this face looks along, and -1 / +1
+};
+
+struct ffv_level_geom {
+  double h;          // cell edge
+  double vol;        // signed volume as meshproperties.c:76-124 computes it
+  double area;       // face area as meshproperties.c:42-73 computes it
+  double inv_unused;
+};
+
+struct ffv_mesh {
+  ffv_forest_desc desc;
+  int64_t n;
+  int32_t nsub;         // number of 4-subface groups
+  int32_t min_level, max_level;
+  uint32_t *info;       // [n]
+  int32_t *nbr;         // [6n]: neighbour cell (kinds 0,1), subface group (kind 2), -1
+  int32_t *sub;         // [4 nsub]
+  int32_t *tree_ijk;    // [3n] canonical order
+  int32_t *cell_ijk;    // [3n]
+  ffv_face_frame frame[6];
+  ffv_level_geom geom[FFV_MAX_LEVEL + 2];
+};

@@ -1,0 +1,146 @@
+/*
+ * ffv.h -- C ABI of the GB300-native explicit finite-volume step of ForestFV.
+ *
+ * This header is the drop-in boundary for the reference's per-RK-stage path, which in
+ * the reference is a set of C calls on a malloc'd leaf linked list:
+ *
+ *   advancetimeexplicit(run)         advancetimeexplicit.c:3-28   -> ffv_step
+ *   RK(irk, run) / m5_RK(irk, run)    RK.c:3-53, m5_RK.c:3-127     -> ffv_stage
+ *   grad_scheme(run)                  grad_scheme.c:3-41           -> (fused into ffv_stage)
+ *   RHS(run)                          RHS.c:3-72                   -> (fused into ffv_stage)
+ *   leaf S[NEQ] arrays (LEAF.S)       strdata.h:233-254            -> ffv_upload_state /
+ *                                                                      ffv_download_state
+ *   neigtr/neigfc/lfc_neigs, CELL     strdata.h:265-332, elconn.c  -> ffv_mesh_build +
+ *     geometry (meshproperties.c)                                      ffv_set_mesh
+ *   global DT (inputset.c:69)         strdata.h:67                 -> dt argument
+ *   globals MODEL, ORDER, RK_STEPS,   strdata.h:45-217             -> ffv_params
+ *     MATERGAMA/MATERPINF ...
+ *
+ * Conventions
+ *   - Cells ("leaves") are numbered in the reference's leaf-list order: trees in the
+ *     order given, then depth-first by child index (rebuildlist.c:30-91).  For a
+ *     Cartesian forest whose trees are listed in Morton order this is a global Morton
+ *     order; ffv_mesh_build returns that order.
+ *   - Conserved state is structure-of-arrays: S[v * ncells + c], v < neq.
+ *   - Every function returns FFV_OK (0) or an FFV_ERR_* code; ffv_error_string names it.
+ *   - A context owns its device memory and one CUDA stream.  It is not thread-safe.
+ *   - No function falls back to the CPU: without a usable CUDA device, ffv_create fails.
+ */
+#ifndef FFV_H
+#define FFV_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFV_OK 0
+#define FFV_ERR_ARG 1          /* bad argument (NULL pointer, size mismatch, bad enum)   */
+#define FFV_ERR_CUDA 2         /* a CUDA runtime call failed                             */
+#define FFV_ERR_TABLE 3        /* mesh description rejected (overlap, hole, range)       */
+#define FFV_ERR_BALANCE 4      /* face neighbours differ by more than one level          */
+#define FFV_ERR_NAN 5          /* non-finite residual or state found on the device       */
+#define FFV_ERR_NEG_DENSITY 6  /* non-positive density found on the device               */
+#define FFV_ERR_TIMEOUT 7      /* a bounded device wait ran out                          */
+#define FFV_ERR_UNSUPPORTED 8  /* option outside what this build implements              */
+#define FFV_ERR_NOMEM 9        /* host or device allocation failed                       */
+#define FFV_ERR_STATE 10       /* call out of order (e.g. step before mesh/state upload) */
+
+#define FFV_MAX_MATERIALS 8
+#define FFV_MAX_NEQ 32
+#define FFV_MAX_LEVEL 15
+
+/* arithmetic of the flux path */
+#define FFV_FP64 0        /* everything in FP64, bit-identical to the reference's C code */
+#define FFV_FP32_FLUX 1   /* reconstruction, wave speeds, HLLC in FP32; FP64 residuals,  */
+                          /* RK state and stiffened-gas pressure recovery                 */
+
+/* boundary codes, as the reference's fc[].bc (m0_bc.c:3-31) */
+#define FFV_BC_SYMMETRY 1
+#define FFV_BC_OUTLET 2     /* transmissive */
+#define FFV_BC_INLET 3
+#define FFV_BC_REFLECTIVE 4
+#define FFV_BC_WALL 5
+
+/* Solver parameters: the reference's input globals for this path. */
+typedef struct ffv_params {
+  int32_t model;        /* MODEL: 0 (Euler, stiffened gas, m0_*) */
+  int32_t nmaterials;   /* NMATERIALS (1 for model 0) */
+  int32_t order;        /* ORDER: 1 (first order) or 2 (MUSCL, GRAD_SCHEME 1) */
+  int32_t rk_steps;     /* RK_STEPS: 1..4; stage k uses the combination of RK.c case k */
+  int32_t precision;    /* FFV_FP64 or FFV_FP32_FLUX */
+  int32_t reserved0;
+  double gamma[FFV_MAX_MATERIALS]; /* MATERGAMA */
+  double pinf[FFV_MAX_MATERIALS];  /* MATERPINF */
+} ffv_params;
+
+/* A Cartesian forest: ntrees[0] x ntrees[1] x ntrees[2] cubic hex trees of edge
+ * tree_edge with corner at the origin, each refined as an octree.  Trees are level 1,
+ * their children level 2, ... (spawntopo.c:136, split.c:25), up to FFV_MAX_LEVEL.
+ * bc[side] gives the boundary code of the domain sides -x,+x,-y,+y,-z,+z.
+ * tree_edge * 2^k must be exact for every level: a power of two times an integer. */
+typedef struct ffv_forest_desc {
+  int32_t ntrees[3];
+  int32_t bc[6];
+  double tree_edge;
+} ffv_forest_desc;
+
+typedef struct ffv_mesh ffv_mesh; /* host-side face tables */
+typedef struct ffv_ctx ffv_ctx;   /* device context */
+
+/* Build the owner-sorted face tables of a 2:1-balanced forest from its leaves.
+ * Leaf i lies in tree (tree_ijk[3i..3i+2]) at `level[i]` with integer coordinates
+ * cell_ijk[3i..3i+2] inside the tree (0 <= c < 2^(level-1)).  Leaves may come in any
+ * order; `order_out` (nleaves entries, may be NULL) receives, for each cell of the
+ * built mesh, the index of the input leaf it holds.  Replaces the reference's
+ * neighbour search (elconn.c:3-145, elconnfin.c) and geometry
+ * (meshproperties.c:3-126, distance.c:120-167) for Cartesian forests. */
+int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves, const int32_t *tree_ijk,
+                   const int32_t *level, const int32_t *cell_ijk, ffv_mesh **out,
+                   int64_t *order_out);
+int64_t ffv_mesh_ncells(const ffv_mesh *m);
+void ffv_mesh_free(ffv_mesh *m);
+
+/* Expand the tables into the reference's per-leaf geometry, for validation against
+ * the reference (one row per cell-face, 6 per cell, in cell order):
+ *   bc, lfc_neigs (0 boundary, 1, 4), neigfc, nb[4] (cell ids, -1 unused),
+ *   area[4], nrm[9] (n, t1, t2 as in normalvector.c / tagvector.c),
+ *   dist_cf, dist_cc (distance.c:120-167); per cell: vol (meshproperties.c:76-124),
+ *   centroid[3] (meshproperties.c:27-38).  Any output pointer may be NULL. */
+int ffv_mesh_export(const ffv_mesh *m, int32_t *bc, int32_t *lfc_neigs, int32_t *neigfc,
+                    int32_t *nb, double *area, double *nrm, double *dist_cf,
+                    double *dist_cc, double *vol, double *centroid);
+
+/* Device context on CUDA device `device`. */
+int ffv_create(ffv_ctx **ctx, const ffv_params *p, int device);
+int ffv_destroy(ffv_ctx *ctx);
+/* Upload the face tables (after every regrid).  Invalidates the state. */
+int ffv_set_mesh(ffv_ctx *ctx, const ffv_mesh *m);
+/* Conserved state, SoA [neq][ncells], host memory, FP64. */
+int ffv_upload_state(ffv_ctx *ctx, const double *S_soa, int64_t ncells, int32_t neq);
+int ffv_download_state(ffv_ctx *ctx, double *S_soa, int64_t ncells, int32_t neq);
+/* One RK stage, the counterpart of RK(irk) / m5_RK(irk) preceded for irk >= 1 by
+ * grad_scheme and RHS (advancetimeexplicit.c:9-19): irk 0 copies S to SN; irk >= 1
+ * reconstructs face states, accumulates face fluxes and applies stage irk.  Queued
+ * on the context's stream; errors seen on the device are reported by ffv_sync. */
+int ffv_stage(ffv_ctx *ctx, int32_t irk, double dt);
+/* nsteps full time steps of rk_steps stages each (advancetimeexplicit x nsteps),
+ * launched as one CUDA graph per step; synchronises and checks the device status. */
+int ffv_step(ffv_ctx *ctx, double dt, int32_t nsteps);
+/* Wait for queued work and return the first error the device recorded. */
+int ffv_sync(ffv_ctx *ctx);
+/* Largest stable dt for the given CFL number: cfl * min over cells of
+ * h / max(|u_a| + c) (new: the reference uses a fixed DT, inputset.c:69). */
+int ffv_cfl_dt(ffv_ctx *ctx, double cfl, double *dt_out);
+/* Device pointer of the conserved state (SoA), valid until the next ffv_set_mesh. */
+int ffv_state_device_ptr(ffv_ctx *ctx, double **d_S);
+/* Number of kernel launches one time step issues (for launch accounting). */
+int ffv_launches_per_step(const ffv_ctx *ctx, int32_t *n);
+
+const char *ffv_error_string(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFV_H */

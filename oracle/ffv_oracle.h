@@ -1,0 +1,57 @@
+/*
+ * CPU restatement of the reference's explicit finite-volume step (TEST INFRASTRUCTURE).
+ *
+ * This is the oracle that the CUDA path is checked against.  It restates, on flat
+ * arrays, the algorithm of the reference's own C code, function by function, with the
+ * same floating-point operation order; it is pinned against the reference itself
+ * (oracle/_ref, built from the reference's sources by oracle/ref/Makefile) by the tests
+ * under tests/.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+ * may load it.  It is never part of the product path.
+ *
+ * Geometry is taken in the reference's own per-leaf form (general hex geometry, no
+ * Cartesian shortcuts), one row per cell face, six rows per cell.
+ */
+#ifndef FFV_ORACLE_H
+#define FFV_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ffvo_mesh {
+  int64_t n;
+  const int32_t *bc;        /* [6n] fc[f].bc                                  */
+  const int32_t *nn;        /* [6n] lfc_neigs[f] (0 on boundary faces)        */
+  const int32_t *neigfc;    /* [6n] neigfc[f]                                 */
+  const int32_t *nb;        /* [24n] neigtr[f][k] as cell index, -1 unused     */
+  const double *area;       /* [24n] Area[f][k]                               */
+  const double *nrm;        /* [54n] nx ny nz, nxt1 nyt1 nzt1, nxt2 nyt2 nzt2 */
+  const double *dist_cf;    /* [6n]                                           */
+  const double *dist_cc;    /* [6n]                                           */
+  const double *vol;        /* [n]  signed Vol                                */
+  const int32_t *si;        /* [n]  SI[0] (interface-layer index), may be NULL */
+} ffvo_mesh;
+
+typedef struct ffvo_params {
+  int32_t order;     /* ORDER 1 or 2 */
+  int32_t rk_steps;  /* RK_STEPS */
+  double gamma;      /* MATERGAMA[0] */
+  double pinf;       /* MATERPINF[0] */
+} ffvo_params;
+
+/* Model 0: advance S (AoS, [n][5]) by nsteps steps of size dt, as loop.c:12-21 ->
+ * advancetimeexplicit.c:9-24 do.  Returns 0, or a nonzero code where the reference
+ * would print and exit (NaN residual, no HLLC branch taken). */
+int ffvo_m0_advance(const ffvo_mesh *m, const ffvo_params *p, double *S, double dt,
+                    int nsteps);
+
+/* Model 0, one stage (irk as RK(irk)); SN, SF, RHS, flux buffers are caller-owned
+ * scratch: SN [n*5], work [n*6*5*2 + n*5 + n*6]. */
+int ffvo_m0_stage(const ffvo_mesh *m, const ffvo_params *p, double *S, double *SN,
+                  double *work, int irk, double dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
