@@ -1,0 +1,95 @@
+"""ctypes binding of the C ABI declared in include/ffv.h.
+
+The shared library is built in-tree (forestfv_public_gb300/_lib/libffv.so, see build.py).
+There is no fallback: if the library is missing or a CUDA device is unusable, loading or
+context creation raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .build import LIB
+
+FFV_MAX_MATERIALS = 8
+FFV_FP64 = 0
+FFV_FP32_FLUX = 1
+
+ERRORS = {
+    0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "mesh description rejected",
+    4: "2:1 balance violated", 5: "non-finite residual or state on the device",
+    6: "non-positive density on the device", 7: "bounded device wait ran out",
+    8: "unsupported option", 9: "out of memory", 10: "call out of order",
+}
+
+
+class FFVError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__(f"{what}: {ERRORS.get(code, 'unknown error')} (code {code})")
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int32), ("nmaterials", ctypes.c_int32),
+                ("order", ctypes.c_int32), ("rk_steps", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("gamma", ctypes.c_double * FFV_MAX_MATERIALS),
+                ("pinf", ctypes.c_double * FFV_MAX_MATERIALS)]
+
+
+class ForestDesc(ctypes.Structure):
+    _fields_ = [("ntrees", ctypes.c_int32 * 3), ("bc", ctypes.c_int32 * 6),
+                ("tree_edge", ctypes.c_double)]
+
+
+_lib = None
+
+EXPORTS = (
+    "ffv_mesh_build", "ffv_mesh_ncells", "ffv_mesh_free", "ffv_mesh_export", "ffv_create",
+    "ffv_destroy", "ffv_set_mesh", "ffv_upload_state", "ffv_download_state", "ffv_stage",
+    "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
+    "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
+)
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        raise RuntimeError(f"{LIB} is not built; run forestfv_public_gb300.build.build() "
+                           "(the CUDA library is required, there is no CPU path)")
+    L = ctypes.CDLL(LIB)
+    vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    L.ffv_mesh_build.argtypes = [ctypes.POINTER(ForestDesc), i64, vp, vp, vp,
+                                 ctypes.POINTER(vp), vp]
+    L.ffv_mesh_ncells.argtypes = [vp]
+    L.ffv_mesh_ncells.restype = i64
+    L.ffv_mesh_free.argtypes = [vp]
+    L.ffv_mesh_free.restype = None
+    L.ffv_mesh_export.argtypes = [vp] + [vp] * 10
+    L.ffv_create.argtypes = [ctypes.POINTER(vp), ctypes.POINTER(Params), ctypes.c_int]
+    L.ffv_destroy.argtypes = [vp]
+    L.ffv_set_mesh.argtypes = [vp, vp]
+    L.ffv_upload_state.argtypes = [vp, vp, i64, i32]
+    L.ffv_download_state.argtypes = [vp, vp, i64, i32]
+    L.ffv_stage.argtypes = [vp, i32, dbl]
+    L.ffv_step.argtypes = [vp, dbl, i32]
+    L.ffv_step_async.argtypes = [vp, dbl, i32]
+    L.ffv_sync.argtypes = [vp]
+    L.ffv_cfl_dt.argtypes = [vp, dbl, ctypes.POINTER(dbl)]
+    L.ffv_state_device_ptr.argtypes = [vp, ctypes.POINTER(vp)]
+    L.ffv_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    L.ffv_profile_stage.argtypes = [vp, i32, dbl, vp, i32, ctypes.POINTER(i32)]
+    L.ffv_stage_kernel_name.argtypes = [vp, i32]
+    L.ffv_stage_kernel_name.restype = ctypes.c_char_p
+    L.ffv_launches_per_step.argtypes = [vp, ctypes.POINTER(i32)]
+    L.ffv_error_string.argtypes = [ctypes.c_int]
+    L.ffv_error_string.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def check(code: int, what: str) -> None:
+    if code != 0:
+        raise FFVError(code, what)

@@ -1,0 +1,404 @@
+// C ABI implementation: device context, table upload, state transfer, stage / step
+// launches (one CUDA graph per time step), CFL reduction, device status word.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+
+#include "ffv_device.cuh"
+
+struct ffv_ctx {
+  ffv_params p;
+  int device;
+  cudaStream_t stream;
+  int64_t n;
+  int32_t neq;
+  int have_mesh, have_state;
+  ffv_dmesh dm;
+  ffv_geom geom;
+  // device buffers
+  uint32_t *d_info;
+  int32_t *d_nbr, *d_sub;
+  double *d_S, *d_SN, *d_SF, *d_dt;
+  unsigned int *d_status;
+  unsigned long long *d_red;
+  // pinned host scalars
+  unsigned int *h_status;
+  unsigned long long *h_red;
+  // one captured time step
+  cudaGraphExec_t graph;
+  int graph_valid;
+};
+
+namespace {
+
+int cuda_rc(cudaError_t e) { return e == cudaSuccess ? FFV_OK : FFV_ERR_CUDA; }
+
+#define CK(x)                                  \
+  do {                                         \
+    cudaError_t e_ = (x);                      \
+    if (e_ != cudaSuccess) return FFV_ERR_CUDA; \
+  } while (0)
+
+void free_mesh_buffers(ffv_ctx *c) {
+  cudaFree(c->d_info);
+  cudaFree(c->d_nbr);
+  cudaFree(c->d_sub);
+  cudaFree(c->d_S);
+  cudaFree(c->d_SN);
+  cudaFree(c->d_SF);
+  c->d_info = nullptr;
+  c->d_nbr = c->d_sub = nullptr;
+  c->d_S = c->d_SN = c->d_SF = nullptr;
+  if (c->graph_valid) cudaGraphExecDestroy(c->graph);
+  c->graph_valid = 0;
+  c->have_mesh = c->have_state = 0;
+}
+
+unsigned status_to_err(unsigned st) {
+  if (st & (FFV_ST_NAN | FFV_ST_NAN_SPEED | FFV_ST_NO_BRANCH)) return FFV_ERR_NAN;
+  if (st & FFV_ST_NEG_DENSITY) return FFV_ERR_NEG_DENSITY;
+  return FFV_OK;
+}
+
+int neq_of(const ffv_params &p) { return p.model == 0 ? 5 : -1; }
+
+int launch_stage(ffv_ctx *c, int irk, cudaEvent_t *ev = nullptr) {
+  ffv_m0_bufs b{c->d_S, c->d_SN, c->d_SF, c->d_dt, c->d_status};
+  ffv_m0_consts k{c->p.gamma[0], c->p.pinf[0], c->p.order};
+  if (irk == 0) {
+    CK(cudaMemcpyAsync(c->d_SN, c->d_S, sizeof(double) * 5 * c->n, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    return FFV_OK;
+  }
+  ffv_m0_fp64_stage(c->dm, c->geom, b, k, irk, c->stream, ev);
+  return cuda_rc(cudaGetLastError());
+}
+
+__global__ void set_scalar(double *dst, double v) { *dst = v; }
+
+int queue_dt(ffv_ctx *c, double dt) {
+  set_scalar<<<1, 1, 0, c->stream>>>(c->d_dt, dt);
+  return cuda_rc(cudaGetLastError());
+}
+
+int build_graph(ffv_ctx *c) {
+  if (c->graph_valid) return FFV_OK;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = FFV_OK;
+  for (int irk = 1; irk <= c->p.rk_steps && rc == FFV_OK; irk++) rc = launch_stage(c, irk);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc != FFV_OK) return rc;
+  CK(e);
+  e = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaGraphDestroy(g);
+  CK(e);
+  c->graph_valid = 1;
+  return FFV_OK;
+}
+
+// CFL: dt = cfl * min over cells of h / max_a(|u_a| + c)  (no reference counterpart:
+// the reference runs with a fixed DT, inputset.c:69)
+__global__ void m0_cfl_kernel(ffv_dmesh m, ffv_geom g, const double *__restrict__ S,
+                              double gamma, double pinf, unsigned long long *out) {
+  double best = INFINITY;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < m.n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int l = ffv_info_level(m.info[c]);
+    const double r = S[c], u = S[m.n + c] / r, v = S[2 * m.n + c] / r, w = S[3 * m.n + c] / r;
+    const double e = S[4 * m.n + c];
+    const double p = r * (gamma - 1.0) * ((e / r) - 0.5 * (u * u + v * v + w * w)) - gamma * pinf;
+    const double a = sqrt(gamma * (p + pinf) / r);
+    const double s = fmax(fmax(fabs(u), fabs(v)), fabs(w)) + a;
+    const double dt = g.h[l] / s;
+    best = (dt < best || isnan(dt)) ? dt : best;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    double other = __shfl_xor_sync(0xffffffffu, best, o);
+    best = (other < best || isnan(other)) ? other : best;
+  }
+  if ((threadIdx.x & 31) == 0) {
+    // non-negative doubles order like their bit patterns; NaN maps above +inf
+    unsigned long long bits = isnan(best) ? 0x7ff8000000000000ULL
+                                          : (unsigned long long)__double_as_longlong(best);
+    if (isnan(best) || best >= 0.0) atomicMin(out, bits);
+    else atomicMin(out, 0ULL);
+  }
+}
+
+}  // namespace
+
+void ffv_m0_cfl(const ffv_dmesh &m, const ffv_geom &g, const double *S, const ffv_m0_consts &k,
+                unsigned long long *d_out, cudaStream_t st) {
+  int blocks = 152 * 4;
+  m0_cfl_kernel<<<blocks, 256, 0, st>>>(m, g, S, k.gamma, k.pinf, d_out);
+}
+
+int ffv_check_frames(const ffv_mesh *m) {
+  for (int f = 0; f < 6; f++) {
+    const ffv_face_frame &fr = m->frame[f];
+    if (fr.n_axis != fr_n_axis(f) || fr.n_sign != fr_n_sign(f) || fr.t1_axis != fr_t1_axis(f) ||
+        fr.t1_sign != fr_t1_sign(f) || fr.t2_axis != fr_t2_axis(f) || fr.t2_sign != fr_t2_sign(f))
+      return FFV_ERR_TABLE;
+  }
+  return FFV_OK;
+}
+
+void ffv_fill_geom(const ffv_mesh *m, ffv_geom *g) {
+  memset(g, 0, sizeof(*g));
+  for (int l = 1; l <= FFV_MAX_LEVEL + 1; l++) {
+    const double h = m->geom[l].h;
+    g->vol[l] = m->geom[l].vol;
+    g->inv_vol[l] = 1.0 / m->geom[l].vol;
+    g->area[l] = m->geom[l].area;
+    g->h[l] = h;
+    // distance.c:120-167, by face class (see ffv_mesh.cpp face_dist)
+    g->dcf[l][0] = 0.5 * h;
+    g->dcc[l][0] = h;
+    const double hp = l > 1 ? m->geom[l - 1].h : 0.0;
+    g->dcf[l][1] = 0.25 * hp;
+    g->dcc[l][1] = 0.25 * hp + 0.5 * hp;
+    g->dcf[l][2] = 0.5 * h;
+    g->dcc[l][2] = 0.5 * h + 0.25 * h;
+    g->dcf[l][3] = 0.0;
+    g->dcc[l][3] = 0.0;
+  }
+}
+
+extern "C" {
+
+const char *ffv_error_string(int code) {
+  switch (code) {
+    case FFV_OK: return "ok";
+    case FFV_ERR_ARG: return "invalid argument";
+    case FFV_ERR_CUDA: return "CUDA runtime error";
+    case FFV_ERR_TABLE: return "mesh description rejected";
+    case FFV_ERR_BALANCE: return "2:1 balance violated";
+    case FFV_ERR_NAN: return "non-finite residual or state on the device";
+    case FFV_ERR_NEG_DENSITY: return "non-positive density on the device";
+    case FFV_ERR_TIMEOUT: return "bounded device wait ran out";
+    case FFV_ERR_UNSUPPORTED: return "unsupported option";
+    case FFV_ERR_NOMEM: return "out of memory";
+    case FFV_ERR_STATE: return "call out of order";
+    default: return "unknown error";
+  }
+}
+
+int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
+  if (!out || !p) return FFV_ERR_ARG;
+  *out = nullptr;
+  if (p->model != 0) return FFV_ERR_UNSUPPORTED;
+  if (p->order != 1 && p->order != 2) return FFV_ERR_ARG;
+  if (p->rk_steps < 1 || p->rk_steps > 4) return FFV_ERR_ARG;
+  if (p->precision != FFV_FP64 && p->precision != FFV_FP32_FLUX) return FFV_ERR_ARG;
+  if (p->precision != FFV_FP64) return FFV_ERR_UNSUPPORTED;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0)
+    return FFV_ERR_CUDA;
+  CK(cudaSetDevice(device));
+  ffv_ctx *c = new (std::nothrow) ffv_ctx();
+  if (!c) return FFV_ERR_NOMEM;
+  memset(c, 0, sizeof(*c));
+  c->p = *p;
+  c->device = device;
+  c->neq = neq_of(*p);
+  int rc = FFV_OK;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_dt, sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->d_status, sizeof(unsigned)) != cudaSuccess ||
+      cudaMalloc(&c->d_red, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost(&c->h_status, sizeof(unsigned)) != cudaSuccess ||
+      cudaMallocHost(&c->h_red, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(c->d_status, 0, sizeof(unsigned)) != cudaSuccess)
+    rc = FFV_ERR_CUDA;
+  if (rc != FFV_OK) {
+    ffv_destroy(c);
+    return rc;
+  }
+  *out = c;
+  return FFV_OK;
+}
+
+int ffv_destroy(ffv_ctx *c) {
+  if (!c) return FFV_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  free_mesh_buffers(c);
+  cudaFree(c->d_dt);
+  cudaFree(c->d_status);
+  cudaFree(c->d_red);
+  cudaFreeHost(c->h_status);
+  cudaFreeHost(c->h_red);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return FFV_OK;
+}
+
+int ffv_set_mesh(ffv_ctx *c, const ffv_mesh *m) {
+  if (!c || !m) return FFV_ERR_ARG;
+  int rc = ffv_check_frames(m);
+  if (rc != FFV_OK) return rc;
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  free_mesh_buffers(c);
+  const int64_t n = m->n;
+  const size_t nsub = (size_t)(m->nsub > 0 ? m->nsub : 1);
+  if (cudaMalloc(&c->d_info, sizeof(uint32_t) * n) != cudaSuccess ||
+      cudaMalloc(&c->d_nbr, sizeof(int32_t) * 6 * n) != cudaSuccess ||
+      cudaMalloc(&c->d_sub, sizeof(int32_t) * 4 * nsub) != cudaSuccess ||
+      cudaMalloc(&c->d_S, sizeof(double) * c->neq * n) != cudaSuccess ||
+      cudaMalloc(&c->d_SN, sizeof(double) * c->neq * n) != cudaSuccess ||
+      cudaMalloc(&c->d_SF, sizeof(double) * 6 * c->neq * n) != cudaSuccess) {
+    free_mesh_buffers(c);
+    return FFV_ERR_NOMEM;
+  }
+  // neighbour slots face-major on the device ([6][n]) for coalesced loads
+  int32_t *nbr_t = (int32_t *)malloc(sizeof(int32_t) * 6 * n);
+  if (!nbr_t) {
+    free_mesh_buffers(c);
+    return FFV_ERR_NOMEM;
+  }
+  for (int64_t i = 0; i < n; i++)
+    for (int f = 0; f < 6; f++) nbr_t[(int64_t)f * n + i] = m->nbr[6 * i + f];
+  cudaError_t e = cudaMemcpy(c->d_info, m->info, sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(c->d_nbr, nbr_t, sizeof(int32_t) * 6 * n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && m->nsub > 0)
+    e = cudaMemcpy(c->d_sub, m->sub, sizeof(int32_t) * 4 * m->nsub, cudaMemcpyHostToDevice);
+  free(nbr_t);
+  if (e != cudaSuccess) {
+    free_mesh_buffers(c);
+    return FFV_ERR_CUDA;
+  }
+  c->n = n;
+  c->dm = ffv_dmesh{n, c->d_info, c->d_nbr, c->d_sub};
+  ffv_fill_geom(m, &c->geom);
+  c->have_mesh = 1;
+  return FFV_OK;
+}
+
+int ffv_upload_state(ffv_ctx *c, const double *S, int64_t ncells, int32_t neq) {
+  if (!c || !S) return FFV_ERR_ARG;
+  if (!c->have_mesh) return FFV_ERR_STATE;
+  if (ncells != c->n || neq != c->neq) return FFV_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(c->d_S, S, sizeof(double) * neq * ncells, cudaMemcpyHostToDevice,
+                     c->stream));
+  CK(cudaMemcpyAsync(c->d_SN, c->d_S, sizeof(double) * neq * ncells, cudaMemcpyDeviceToDevice,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->have_state = 1;
+  return FFV_OK;
+}
+
+int ffv_download_state(ffv_ctx *c, double *S, int64_t ncells, int32_t neq) {
+  if (!c || !S) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  if (ncells != c->n || neq != c->neq) return FFV_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(S, c->d_S, sizeof(double) * neq * ncells, cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return FFV_OK;
+}
+
+int ffv_stage(ffv_ctx *c, int32_t irk, double dt) {
+  if (!c) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  if (irk < 0 || irk > 4) return FFV_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  int rc = queue_dt(c, dt);
+  if (rc != FFV_OK) return rc;
+  return launch_stage(c, irk);
+}
+
+int ffv_sync(ffv_ctx *c) {
+  if (!c) return FFV_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(c->h_status, c->d_status, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return (int)status_to_err(*c->h_status);
+}
+
+int ffv_step_async(ffv_ctx *c, double dt, int32_t nsteps) {
+  if (!c || nsteps < 0) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  CK(cudaSetDevice(c->device));
+  int rc = build_graph(c);
+  if (rc != FFV_OK) return rc;
+  rc = queue_dt(c, dt);
+  if (rc != FFV_OK) return rc;
+  for (int s = 0; s < nsteps; s++) CK(cudaGraphLaunch(c->graph, c->stream));
+  return FFV_OK;
+}
+
+int ffv_step(ffv_ctx *c, double dt, int32_t nsteps) {
+  int rc = ffv_step_async(c, dt, nsteps);
+  if (rc != FFV_OK) return rc;
+  return ffv_sync(c);
+}
+
+int ffv_cfl_dt(ffv_ctx *c, double cfl, double *dt_out) {
+  if (!c || !dt_out || !(cfl > 0.0)) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemsetAsync(c->d_red, 0xff, sizeof(unsigned long long), c->stream));
+  ffv_m0_consts k{c->p.gamma[0], c->p.pinf[0], c->p.order};
+  ffv_m0_cfl(c->dm, c->geom, c->d_S, k, c->d_red, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->h_red, c->d_red, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  double m;
+  memcpy(&m, c->h_red, sizeof(double));
+  if (!(m > 0.0) || isnan(m)) return FFV_ERR_NAN;
+  *dt_out = cfl * m;
+  return FFV_OK;
+}
+
+int ffv_state_device_ptr(ffv_ctx *c, double **d_S) {
+  if (!c || !d_S) return FFV_ERR_ARG;
+  if (!c->have_mesh) return FFV_ERR_STATE;
+  *d_S = c->d_S;
+  return FFV_OK;
+}
+
+int ffv_profile_stage(ffv_ctx *c, int32_t irk, double dt, float *ms, int32_t max_kernels,
+                      int32_t *nkernels) {
+  if (!c || !ms || !nkernels || irk < 1 || irk > 4) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  const int nk = ffv_m0_launches_per_stage(c->p.order);
+  if (max_kernels < nk) return FFV_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  cudaEvent_t ev[8];
+  for (int i = 0; i <= nk; i++) CK(cudaEventCreate(&ev[i]));
+  int rc = queue_dt(c, dt);
+  if (rc == FFV_OK) rc = launch_stage(c, irk, ev);
+  if (rc == FFV_OK && cudaEventSynchronize(ev[nk]) != cudaSuccess) rc = FFV_ERR_CUDA;
+  for (int i = 0; i < nk && rc == FFV_OK; i++)
+    if (cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]) != cudaSuccess) rc = FFV_ERR_CUDA;
+  for (int i = 0; i <= nk; i++) cudaEventDestroy(ev[i]);
+  *nkernels = nk;
+  return rc;
+}
+
+const char *ffv_stage_kernel_name(const ffv_ctx *c, int32_t i) {
+  return c ? ffv_m0_fp64_kernel_name(c->p.order, i) : "";
+}
+
+int ffv_stream(ffv_ctx *c, void **stream) {
+  if (!c || !stream) return FFV_ERR_ARG;
+  *stream = (void *)c->stream;
+  return FFV_OK;
+}
+
+int ffv_launches_per_step(const ffv_ctx *c, int32_t *n) {
+  if (!c || !n) return FFV_ERR_ARG;
+  *n = c->p.rk_steps * ffv_m0_launches_per_stage(c->p.order);
+  return FFV_OK;
+}
+
+}  // extern "C"

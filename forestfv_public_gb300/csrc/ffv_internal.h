@@ -4,14 +4,20 @@
 
 #include "../../include/ffv.h"
 
+#ifdef __CUDACC__
+#define FFV_HD __host__ __device__
+#else
+#define FFV_HD
+#endif
+
 // Face kinds, 4 bits per face in a cell's info word (bits 4f..4f+3); level in bits 24..31.
 #define FFV_FK_SAME 0u     // one neighbour, same level (1:1 face)
 #define FFV_FK_COARSER 1u  // one neighbour, one level coarser (this cell is the fine side)
 #define FFV_FK_FINER 2u    // four neighbours, one level finer (subfaces)
 #define FFV_FK_BC 8u       // boundary: 8 | bc code
 
-static inline uint32_t ffv_face_kind(uint32_t info, int f) { return (info >> (4 * f)) & 15u; }
-static inline int ffv_info_level(uint32_t info) { return (int)(info >> 24); }
+FFV_HD static inline uint32_t ffv_face_kind(uint32_t info, int f) { return (info >> (4 * f)) & 15u; }
+FFV_HD static inline int ffv_info_level(uint32_t info) { return (int)(info >> 24); }
 
 // Hex corner k of a tree or child sits at (x, y, z) = (bit1(k), bit0(k), bit2(k)).  This is
 // the node order under which the reference's face normals (normalvector.c:23-29 applied to

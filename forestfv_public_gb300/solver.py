@@ -1,0 +1,107 @@
+"""Host-side mirror of the reference's per-stage interface, over the C ABI.
+
+  Solver.rk(irk, dt)            RK(irk, run) / m5_RK (RK.c:3-53), preceded for irk >= 1
+                                by grad_scheme (grad_scheme.c:3-41) and RHS (RHS.c:3-72)
+  Solver.advancetimeexplicit(dt) one step of RK_STEPS stages (advancetimeexplicit.c:3-28)
+  Solver.step(dt, n)            n steps, each one CUDA graph launch
+  Solver.cfl_dt(cfl)            CFL time step (the reference has a fixed DT)
+
+State is structure-of-arrays, S[v, c], in the mesh's cell order.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .mesh import Mesh
+
+
+class Solver:
+    def __init__(self, model: int = 0, order: int = 2, rk_steps: int = 2, gamma=(1.4,),
+                 pinf=(0.0,), precision: int = _lib.FFV_FP64, device: int = 0):
+        L = _lib.lib()
+        p = _lib.Params()
+        p.model, p.nmaterials, p.order, p.rk_steps, p.precision = model, len(gamma), order, rk_steps, precision
+        for i, g in enumerate(gamma):
+            p.gamma[i] = g
+        for i, q in enumerate(pinf):
+            p.pinf[i] = q
+        self.params = p
+        self.neq = 5 if model == 0 else None
+        h = ctypes.c_void_p()
+        _lib.check(L.ffv_create(ctypes.byref(h), ctypes.byref(p), device), "ffv_create")
+        self._h = h
+        self.mesh: Mesh | None = None
+
+    def set_mesh(self, mesh: Mesh) -> None:
+        _lib.check(_lib.lib().ffv_set_mesh(self._h, mesh.handle), "ffv_set_mesh")
+        self.mesh = mesh
+
+    def upload_state(self, S: np.ndarray) -> None:
+        S = np.ascontiguousarray(S, dtype=np.float64)
+        assert S.shape == (self.neq, self.mesh.n), S.shape
+        _lib.check(_lib.lib().ffv_upload_state(self._h, S.ctypes.data, self.mesh.n, self.neq),
+                   "ffv_upload_state")
+
+    def download_state(self) -> np.ndarray:
+        S = np.empty((self.neq, self.mesh.n))
+        _lib.check(_lib.lib().ffv_download_state(self._h, S.ctypes.data, self.mesh.n, self.neq),
+                   "ffv_download_state")
+        return S
+
+    def rk(self, irk: int, dt: float) -> None:
+        _lib.check(_lib.lib().ffv_stage(self._h, irk, dt), "ffv_stage")
+
+    def sync(self) -> None:
+        _lib.check(_lib.lib().ffv_sync(self._h), "ffv_sync")
+
+    def advancetimeexplicit(self, dt: float) -> None:
+        self.step(dt, 1)
+
+    def step(self, dt: float, nsteps: int = 1) -> None:
+        _lib.check(_lib.lib().ffv_step(self._h, dt, nsteps), "ffv_step")
+
+    def step_async(self, dt: float, nsteps: int = 1) -> None:
+        _lib.check(_lib.lib().ffv_step_async(self._h, dt, nsteps), "ffv_step_async")
+
+    def cfl_dt(self, cfl: float) -> float:
+        out = ctypes.c_double()
+        _lib.check(_lib.lib().ffv_cfl_dt(self._h, cfl, ctypes.byref(out)), "ffv_cfl_dt")
+        return out.value
+
+    def launches_per_step(self) -> int:
+        n = ctypes.c_int32()
+        _lib.check(_lib.lib().ffv_launches_per_step(self._h, ctypes.byref(n)), "ffv_launches_per_step")
+        return n.value
+
+    def profile_stage(self, irk: int, dt: float) -> dict:
+        """Per-kernel durations (ms) of one stage, CUDA events on the solver's stream."""
+        ms = np.zeros(8, dtype=np.float32)
+        nk = ctypes.c_int32()
+        L = _lib.lib()
+        _lib.check(L.ffv_profile_stage(self._h, irk, dt, ms.ctypes.data, 8, ctypes.byref(nk)),
+                   "ffv_profile_stage")
+        return {L.ffv_stage_kernel_name(self._h, i).decode(): float(ms[i]) for i in range(nk.value)}
+
+    def stream_handle(self) -> int:
+        p = ctypes.c_void_p()
+        _lib.check(_lib.lib().ffv_stream(self._h, ctypes.byref(p)), "ffv_stream")
+        return p.value
+
+    def device_state_ptr(self) -> int:
+        p = ctypes.c_void_p()
+        _lib.check(_lib.lib().ffv_state_device_ptr(self._h, ctypes.byref(p)), "ffv_state_device_ptr")
+        return p.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.lib().ffv_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -128,6 +128,8 @@ int ffv_stage(ffv_ctx *ctx, int32_t irk, double dt);
 /* nsteps full time steps of rk_steps stages each (advancetimeexplicit x nsteps),
  * launched as one CUDA graph per step; synchronises and checks the device status. */
 int ffv_step(ffv_ctx *ctx, double dt, int32_t nsteps);
+/* As ffv_step, but only queues the graph launches on the context's stream. */
+int ffv_step_async(ffv_ctx *ctx, double dt, int32_t nsteps);
 /* Wait for queued work and return the first error the device recorded. */
 int ffv_sync(ffv_ctx *ctx);
 /* Largest stable dt for the given CFL number: cfl * min over cells of
@@ -135,6 +137,14 @@ int ffv_sync(ffv_ctx *ctx);
 int ffv_cfl_dt(ffv_ctx *ctx, double cfl, double *dt_out);
 /* Device pointer of the conserved state (SoA), valid until the next ffv_set_mesh. */
 int ffv_state_device_ptr(ffv_ctx *ctx, double **d_S);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their own work or
+ * timing events against the solver's. */
+int ffv_stream(ffv_ctx *ctx, void **stream);
+/* Diagnostic timing: run stage irk (>= 1) with a CUDA event around each kernel it
+ * launches; ms[i] receives kernel i's duration, *nkernels their count. */
+int ffv_profile_stage(ffv_ctx *ctx, int32_t irk, double dt, float *ms, int32_t max_kernels,
+                      int32_t *nkernels);
+const char *ffv_stage_kernel_name(const ffv_ctx *ctx, int32_t i);
 /* Number of kernel launches one time step issues (for launch accounting). */
 int ffv_launches_per_step(const ffv_ctx *ctx, int32_t *n);
 

@@ -1,0 +1,81 @@
+"""ctypes binding of the CPU restatement (oracle/_build/libffv_oracle.so).
+
+TEST INFRASTRUCTURE: the checker for the CUDA path, used only by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libffv_oracle.so")
+
+_lib = None
+
+
+class _Mesh(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64)] + [(k, ctypes.c_void_p) for k in (
+        "bc", "nn", "neigfc", "nb", "area", "nrm", "dist_cf", "dist_cc", "vol", "si")]
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int32), ("rk_steps", ctypes.c_int32),
+                ("gamma", ctypes.c_double), ("pinf", ctypes.c_double)]
+
+
+def build() -> str:
+    srcs = sorted(os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".c"))
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    cmd = ["gcc", "-std=c99", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+           "-o", LIB, *srcs, "-lm"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return LIB
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = ctypes.CDLL(LIB)
+        L.ffvo_m0_advance.argtypes = [ctypes.POINTER(_Mesh), ctypes.POINTER(_Params),
+                                      ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+class OracleMesh:
+    """Reference-form geometry (keys as Mesh.export() / the reference dump)."""
+
+    def __init__(self, g: dict, si=None):
+        self._keep = {}
+
+        def P(name, a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            self._keep[name] = a
+            return a.ctypes.data
+
+        n = int(np.asarray(g["vol"]).shape[0])
+        self.n = n
+        self.c = _Mesh(n=n, bc=P("bc", g["bc"], np.int32), nn=P("nn", g["nn"], np.int32),
+                       neigfc=P("neigfc", g["neigfc"], np.int32), nb=P("nb", g["nb"], np.int32),
+                       area=P("area", g["area"], np.float64), nrm=P("nrm", g["nrm"], np.float64),
+                       dist_cf=P("dist_cf", g["dist_cf"], np.float64),
+                       dist_cc=P("dist_cc", g["dist_cc"], np.float64),
+                       vol=P("vol", g["vol"], np.float64),
+                       si=P("si", np.zeros(n) if si is None else si, np.int32))
+
+
+def m0_advance(mesh: OracleMesh, S_aos: np.ndarray, dt: float, nsteps: int, order: int = 2,
+               rk_steps: int = 2, gamma: float = 1.4, pinf: float = 0.0) -> np.ndarray:
+    """Advance an AoS [n,5] state; returns the new state (input untouched)."""
+    S = np.ascontiguousarray(S_aos, dtype=np.float64).copy()
+    p = _Params(order=order, rk_steps=rk_steps, gamma=gamma, pinf=pinf)
+    err = lib().ffvo_m0_advance(ctypes.byref(mesh.c), ctypes.byref(p), S.ctypes.data, dt, nsteps)
+    if err:
+        raise RuntimeError(f"oracle stopped with code {err} (the reference would exit here)")
+    return S

@@ -1,0 +1,87 @@
+"""Generate the golden fixtures under tests/golden/ by running the reference solver's own
+C code (built single-rank into oracle/_ref by oracle/ref/Makefile) on synthetic cases.
+
+Each fixture holds the case parameters, the reference's leaf list (tree index, level,
+child-index path), its initial and final conserved state, its loop time, and -- for the
+small cases -- its per-leaf geometry (neighbours, areas, normals, distances, volume), so
+that the CPU restatement, the face-table builder and the CUDA path can be checked
+against the reference on a machine where the reference is not available.
+
+Usage: python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import refcase as rc  # noqa: E402
+
+SOD = "split 0 0.5 1 0 0 0 1 0.125 0 0 0 0.1"
+
+# name -> (Case, keep geometry)
+CASES = {
+    "m0_sod_uniform": (rc.Case(trees=(4, 4, 4), level=2, steps=20, dt=0.002, ic=SOD), True),
+    "m0_sphere_amr": (rc.Case(trees=(2, 2, 2), level=3, steps=10, dt=0.001,
+                              refine="sphere 0.5 0.5 0.5 0.3 4 3",
+                              ic="sphere 0.5 0.5 0.5 0.2 1 0 0 0 1 0.125 0 0 0 0.1"), True),
+    "m0_wave_box_mixedbc": (rc.Case(trees=(4, 4, 4), level=2, steps=10, dt=0.001,
+                                    refine="box 0.1 0.2 0.3 0.6 0.7 0.9 4 2",
+                                    bc=(2, 4, 2, 4, 1, 2), ic="wave 1 0.1 -0.2 0.3 1 0.2 1 2 1"),
+                            True),
+    "m0_wave_order1_rk3_reflective": (rc.Case(trees=(4, 4, 4), level=2, steps=10, dt=0.001,
+                                              rk_steps=3, order=1, bc=(4,) * 6,
+                                              ic="wave 1 0.1 -0.2 0.3 1 0.2 1 2 1"), True),
+    "m0_stiff_rk4_allbc": (rc.Case(trees=(4, 4, 4), level=2, steps=10, dt=0.0005, rk_steps=4,
+                                   gamma=4.4, pinf=6.0, bc=(1, 2, 3, 4, 1, 2),
+                                   ic="wave 1 0.1 -0.2 0.3 20 0.2 1 2 1"), True),
+    "m0_blast_amr_deep": (rc.Case(trees=(2, 2, 2), level=2, steps=8, dt=0.0005,
+                                  refine="sphere 0.3 0.6 0.4 0.35 5 2",
+                                  ic="sphere 0.3 0.6 0.4 0.2 1 0.5 -0.3 0.2 10 1 0 0 0 1"), True),
+}
+
+
+def config1_case() -> rc.Case:
+    """Plain-method Sod problem of the 32^3 uniform forest: 4^3 trees at level 4, ideal
+    gas, transmissive, MUSCL-HLLC, RK_STEPS 2, 100 steps.  The reference has no CFL
+    logic (DT is an input, inputset.c:69): dt is CFL 0.4 on the initial state,
+    0.4 * h / max(|u| + c) with h = 1/32 and c = sqrt(1.4) on the left state."""
+    h = 1.0 / 32.0
+    dt = 0.4 * h / np.sqrt(1.4)
+    return rc.Case(trees=(4, 4, 4), level=4, steps=100, dt=float(dt), ic=SOD)
+
+
+def save(name: str, c: rc.Case, keep_geom: bool) -> None:
+    init, final, _ = rc.run_case(c)
+    d = dict(
+        ntrees=np.array(c.trees, np.int32), bc_sides=np.array(c.bc, np.int32),
+        steps=np.int32(c.steps), dt=np.float64(c.dt), rk_steps=np.int32(c.rk_steps),
+        order=np.int32(c.order), gamma=np.float64(c.gamma), pinf=np.float64(c.pinf),
+        root=final.root, level=final.level, adrs=final.adrs.astype(np.int8),
+        S_init=init.S, S_final=final.S, ref_loop_seconds=np.float64(final.loop_seconds),
+    )
+    if keep_geom:
+        d.update(bc=final.bc.astype(np.int8), nn=final.nneig.astype(np.int8),
+                 neigfc=final.neigfc.astype(np.int8), nb=final.nb, area=final.area,
+                 nrm=final.normals.astype(np.int8), dist_cf=final.dist_cf,
+                 dist_cc=final.dist_cc, vol=final.vol, xc=final.xc)
+        assert np.array_equal(d["nrm"].astype(np.float64), final.normals)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+    print(f"{name}: {final.n} leaves, {c.steps} steps, reference loop {final.loop_seconds:.3f} s")
+
+
+def main() -> None:
+    if not rc.build_ref():
+        raise SystemExit("reference oracle could not be built")
+    for name, (c, g) in CASES.items():
+        save(name, c, g)
+    save("m0_config1_sod32", config1_case(), False)
+
+
+if __name__ == "__main__":
+    main()
