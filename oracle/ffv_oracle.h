@@ -51,6 +51,29 @@ int ffvo_m0_advance(const ffvo_mesh *m, const ffvo_params *p, double *S, double 
 int ffvo_m0_stage(const ffvo_mesh *m, const ffvo_params *p, double *S, double *SN,
                   double *work, int irk, double dt);
 
+/* Model 5 (m5_*): N materials, NEQ = 3N + 12. */
+typedef struct ffvo_m5_params {
+  int32_t nmat;      /* NMATERIALS (2..4) */
+  int32_t order;     /* ORDER */
+  int32_t rk_steps;  /* RK_STEPS */
+  int32_t prelax;    /* PRELAX: 1 (two materials, closed form) or 3 (iterative) */
+  int32_t zerou[3];  /* ZEROU0..2 */
+  int32_t reserved;
+  double gamma[4], pinf[4], mu[4];  /* MATERGAMA, MATERPINF, MATERMUSH */
+  double amin;       /* AMIN */
+  double avf_lim;    /* AVF_LIM */
+} ffvo_m5_params;
+
+/* Advance S (AoS, [n][3N+12]) by nsteps steps of size dt (loop.c:12-21 ->
+ * advancetimeexplicit.c:9-24 with m5_RK and m5_relaxation_solid).  Returns 0 or the
+ * code of the check where the reference would print and exit. */
+int ffvo_m5_advance(const ffvo_mesh *m, const ffvo_m5_params *p, double *S, double dt,
+                    int nsteps);
+
+/* Number of ghost-fluid velocity fixes run so far (m5_gfm: relax 0, m5_gfm_rel: 1), so
+ * that tests can show a case exercises them. */
+long ffvo_m5_gfm_calls(int relax);
+
 #ifdef __cplusplus
 }
 #endif

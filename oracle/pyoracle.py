@@ -27,6 +27,14 @@ class _Params(ctypes.Structure):
                 ("gamma", ctypes.c_double), ("pinf", ctypes.c_double)]
 
 
+class _M5Params(ctypes.Structure):
+    _fields_ = [("nmat", ctypes.c_int32), ("order", ctypes.c_int32), ("rk_steps", ctypes.c_int32),
+                ("prelax", ctypes.c_int32), ("zerou", ctypes.c_int32 * 3),
+                ("reserved", ctypes.c_int32), ("gamma", ctypes.c_double * 4),
+                ("pinf", ctypes.c_double * 4), ("mu", ctypes.c_double * 4),
+                ("amin", ctypes.c_double), ("avf_lim", ctypes.c_double)]
+
+
 def build() -> str:
     srcs = sorted(os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith(".c"))
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
@@ -44,8 +52,17 @@ def lib() -> ctypes.CDLL:
         L = ctypes.CDLL(LIB)
         L.ffvo_m0_advance.argtypes = [ctypes.POINTER(_Mesh), ctypes.POINTER(_Params),
                                       ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        L.ffvo_m5_advance.argtypes = [ctypes.POINTER(_Mesh), ctypes.POINTER(_M5Params),
+                                      ctypes.c_void_p, ctypes.c_double, ctypes.c_int]
+        L.ffvo_m5_gfm_calls.restype = ctypes.c_long
+        L.ffvo_m5_gfm_calls.argtypes = [ctypes.c_int]
         _lib = L
     return _lib
+
+
+def m5_gfm_calls() -> tuple[int, int]:
+    """(m5_gfm, m5_gfm_rel) invocations of the model-5 restatement in this process."""
+    return int(lib().ffvo_m5_gfm_calls(0)), int(lib().ffvo_m5_gfm_calls(1))
 
 
 class OracleMesh:
@@ -76,6 +93,21 @@ def m0_advance(mesh: OracleMesh, S_aos: np.ndarray, dt: float, nsteps: int, orde
     S = np.ascontiguousarray(S_aos, dtype=np.float64).copy()
     p = _Params(order=order, rk_steps=rk_steps, gamma=gamma, pinf=pinf)
     err = lib().ffvo_m0_advance(ctypes.byref(mesh.c), ctypes.byref(p), S.ctypes.data, dt, nsteps)
+    if err:
+        raise RuntimeError(f"oracle stopped with code {err} (the reference would exit here)")
+    return S
+
+
+def m5_advance(mesh: OracleMesh, S_aos: np.ndarray, dt: float, nsteps: int, m5: dict,
+               order: int = 2, rk_steps: int = 2, zerou=(0, 0, 0)) -> np.ndarray:
+    """Model 5: advance an AoS [n, 3N+12] state; returns the new state."""
+    S = np.ascontiguousarray(S_aos, dtype=np.float64).copy()
+    p = _M5Params(nmat=len(m5["gamma"]), order=order, rk_steps=rk_steps, prelax=m5["prelax"],
+                  amin=m5["amin"], avf_lim=m5["avf_lim"])
+    p.zerou[:] = zerou
+    for i, (g, q, mu) in enumerate(zip(m5["gamma"], m5["pinf"], m5["mu"])):
+        p.gamma[i], p.pinf[i], p.mu[i] = g, q, mu
+    err = lib().ffvo_m5_advance(ctypes.byref(mesh.c), ctypes.byref(p), S.ctypes.data, dt, nsteps)
     if err:
         raise RuntimeError(f"oracle stopped with code {err} (the reference would exit here)")
     return S

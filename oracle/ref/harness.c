@@ -198,10 +198,81 @@ void __wrap_loop(struct RUN *run) {
   dump(run, "final", t1 - t0, (int64_t)NSTEP + 1);
 }
 
-/* m5_init_domain.c does not compile as published; model-5 parity cases supply their
- * initial state through the harness (filled in with the model-5 oracle). */
+/* m5_init_domain.c does not compile as published; this replacement assigns each leaf one
+ * material by geometric regions read from <case>.ic and fills its state with the
+ * reference's own m5_init_S (init_S.c:205-266):
+ *   m5 default_mat nregions  then per region one of
+ *      sphere cx cy cz r mat       |   below axis x0 mat   |   above axis x0 mat
+ * The first region that contains the leaf centroid wins. */
+void m5_init_S(struct RUN *run, struct BRANCH *crnt, int mat);
 void m5_init_domain(struct RUN *run) {
-  (void)run;
-  fprintf(stderr, "harness: model-5 initial conditions are not available in this build\n");
-  exit(3);
+  FILE *fp = open_case_file(run, ".ic");
+  if (!fp) { fprintf(stderr, "harness: model 5 needs <case>.ic\n"); exit(3); }
+  char kind[64];
+  int defmat = 0, nreg = 0;
+  if (fscanf(fp, "%63s %d %d", kind, &defmat, &nreg) != 3 || strcmp(kind, "m5")) {
+    fprintf(stderr, "harness: bad model-5 .ic\n"); exit(3);
+  }
+  char rk[16][16];
+  double ra[16][6];
+  int rm[16];
+  for (int i = 0; i < nreg && i < 16; i++) {
+    if (fscanf(fp, "%15s", rk[i]) != 1) exit(3);
+    int np = !strcmp(rk[i], "sphere") ? 4 : 2;
+    for (int j = 0; j < np; j++) if (fscanf(fp, "%lf", &ra[i][j]) != 1) exit(3);
+    if (fscanf(fp, "%d", &rm[i]) != 1) exit(3);
+  }
+  fclose(fp);
+  for (struct BRANCH *c = run->topo->locl; c; c = c->lnxt) {
+    double x[3] = {c->cl->xc, c->cl->yc, c->cl->zc};
+    int mat = defmat;
+    for (int i = 0; i < nreg; i++) {
+      int in;
+      if (!strcmp(rk[i], "sphere")) {
+        double d2 = (x[0] - ra[i][0]) * (x[0] - ra[i][0]) + (x[1] - ra[i][1]) * (x[1] - ra[i][1]) +
+                    (x[2] - ra[i][2]) * (x[2] - ra[i][2]);
+        in = d2 < ra[i][3] * ra[i][3];
+      } else if (!strcmp(rk[i], "below")) {
+        in = x[(int)ra[i][0]] < ra[i][1];
+      } else {
+        in = x[(int)ra[i][0]] > ra[i][1];
+      }
+      if (in) { mat = rm[i]; break; }
+    }
+    for (int iv = 0; iv < NEQ; iv++) c->el->S[iv] = 0.0;
+    m5_init_S(run, c, mat);
+  }
+  /* optional <case>.mix: axis lo hi mat_a alpha_a mat_b p u v w -- cells whose centroid
+   * lies in [lo, hi) along axis hold a two-material mixture at pressure p, velocity
+   * (u,v,w), the remaining materials at AMIN, deformation A = I (so no elastic energy) */
+  fp = open_case_file(run, ".mix");
+  if (!fp) return;
+  double mx[10];
+  int nm = 0;
+  while (nm < 10 && fscanf(fp, "%lf", &mx[nm]) == 1) nm++;
+  fclose(fp);
+  if (nm != 10) { fprintf(stderr, "harness: bad .mix\n"); exit(3); }
+  int ax = (int)mx[0], ma = (int)mx[3], mb = (int)mx[5];
+  for (struct BRANCH *c = run->topo->locl; c; c = c->lnxt) {
+    double x[3] = {c->cl->xc, c->cl->yc, c->cl->zc};
+    if (!(x[ax] >= mx[1] && x[ax] < mx[2])) continue;
+    double a[10], rho = 0.0, E = 0.0;
+    for (int k = 0; k < NMATERIALS; k++) a[k] = AMIN;
+    a[ma] = mx[4];
+    a[mb] = 1.0 - mx[4] - (double)(NMATERIALS - 2) * AMIN;
+    for (int k = 0; k < NMATERIALS; k++) {
+      double ar = a[k] * MATERRINI[k];
+      double are = a[k] * (mx[6] + MATERGAMA[k] * MATERPINF[k]) / (MATERGAMA[k] - 1.0);
+      c->el->S[eqtypi[0] + k] = ar;
+      c->el->S[eqtypi[4] + k] = are;
+      rho += ar;
+      E += are;
+    }
+    for (int k = 0; k < NMATERIALS - 1; k++) c->el->S[eqtypi[3] + k] = a[k];
+    c->el->S[eqtypi[1] + 0] = rho * mx[7];
+    c->el->S[eqtypi[1] + 1] = rho * mx[8];
+    c->el->S[eqtypi[1] + 2] = rho * mx[9];
+    c->el->S[eqtypi[2]] = E + 0.5 * rho * (mx[7] * mx[7] + mx[8] * mx[8] + mx[9] * mx[9]);
+    for (int q = 0; q < 9; q++) c->el->S[eqtypi[5] + q] = (q % 4 == 0) ? 1.0 : 0.0;
+  }
 }

@@ -93,6 +93,13 @@ class Case:
     bc: tuple[int, ...] = (2, 2, 2, 2, 2, 2)   # per side -x,+x,-y,+y,-z,+z
     layout: tuple = LAYOUT_INWARD
     extra: dict = field(default_factory=dict)
+    # model 5: dict with avf_lim, prelax, amin and per-material lists pinf, gamma, mu,
+    # rho0, p0 (u0, v0, w0 optional, >= 0 as m5_input.c:113-135 checks them)
+    m5: dict | None = None
+
+    @property
+    def neq(self) -> int:
+        return 5 if self.model == 0 else 3 * len(self.m5["gamma"]) + 12
 
 
 def _ct_lines(c: Case, levels: int) -> list[str]:
@@ -165,6 +172,20 @@ def write_case(c: Case, d: str, name: str = "case") -> str:
         levels = max(levels, max(int(float(t)) for t in toks[-2:]))
     with open(base + ".ct", "w") as f:
         f.write("\n".join(_ct_lines(c, levels)) + "\n")
+        if c.model == 5:
+            q = c.m5
+            nm = len(q["gamma"])
+
+            def row(name, vals):
+                return name + "".join(f"\t{v:.17e}" for v in vals) + "\n"
+
+            f.write(f"AVF_LIM\t{q['avf_lim']:.17e}\nPRELAX\t{q['prelax']}\n")
+            f.write(f"NMATERIALS\t{nm}\nAMIN\t{q['amin']:.17e}\n")
+            f.write("CRT_ADAPT_INTER_0\t0\t0\t0\nCRT_ADAPT_INTER_1\t0\t0\t0\n")
+            f.write(row("P_INF", q["pinf"]) + row("GAMMA", q["gamma"]) + row("MU", q["mu"]))
+            f.write(row("VISC", [0.0] * nm) + row("RHO_INIT", q["rho0"]) + row("PR_INIT", q["p0"]))
+            for key in ("u0", "v0", "w0"):
+                f.write(row(key.upper(), q.get(key, [0.0] * nm)))
     if c.model == 0:
         with open(base + ".m0ct", "w") as f:
             f.write("".join(f"SKIP{i}\t0\n" for i in range(31)))
@@ -174,6 +195,9 @@ def write_case(c: Case, d: str, name: str = "case") -> str:
     if c.refine:
         with open(base + ".rf", "w") as f:
             f.write(c.refine + "\n")
+    if c.m5 and c.m5.get("mix"):
+        with open(base + ".mix", "w") as f:
+            f.write(c.m5["mix"] + "\n")
     return base
 
 

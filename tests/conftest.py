@@ -15,16 +15,24 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run on the GB300 box)")
 
 
-def golden_names(with_geometry=None):
+def golden_names(with_geometry=None, model=None):
     out = []
     for p in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         name = os.path.splitext(os.path.basename(p))[0]
-        if with_geometry is not None:
-            has = "nb" in np.load(p).files
-            if has != with_geometry:
-                continue
+        z = np.load(p)
+        if with_geometry is not None and ("nb" in z.files) != with_geometry:
+            continue
+        if model is not None and int(z["model"]) != model:
+            continue
         out.append(name)
     return out
+
+
+def m5_params(g):
+    """Model-5 material parameters of a fixture, as oracle/pyoracle.m5_advance takes them."""
+    return dict(avf_lim=float(g["m5_avf_lim"]), prelax=int(g["m5_prelax"]),
+                amin=float(g["m5_amin"]), pinf=list(g["m5_pinf"]), gamma=list(g["m5_gamma"]),
+                mu=list(g["m5_mu"]))
 
 
 def load_golden(name):

@@ -46,6 +46,36 @@ CASES = {
 }
 
 
+WALL = dict(avf_lim=0.5, prelax=3, amin=1e-6, pinf=[3.2e10, 6e8, 0.0], gamma=[3.5, 4.4, 1.4],
+            mu=[2.6e10, 0.0, 0.0], rho0=[2700.0, 1000.0, 1.0], p0=[5e6, 5e6, 1e5])
+WALL_IC = "m5 1 2 below 2 0.25 0 sphere 0.5 0.5 0.6 0.15 2"
+
+M5_CASES = {
+    # liquid (stiffened gas) with a gas sphere, sharp interface, iterative relaxation
+    "m5_bubble_prelax3": rc.Case(trees=(2, 2, 2), level=3, steps=3, dt=1e-7, model=5,
+                                 m5=dict(avf_lim=1.0, prelax=3, amin=1e-6, pinf=[6e8, 0.0],
+                                         gamma=[4.4, 1.4], mu=[0.0, 0.0], rho0=[1000.0, 1.0],
+                                         p0=[5e6, 1e5]),
+                                 ic="m5 0 1 sphere 0.5 0.5 0.5 0.2 1"),
+    # two mild materials, closed-form two-material relaxation
+    "m5_mild_prelax1": rc.Case(trees=(2, 2, 2), level=3, steps=3, dt=1e-3, model=5,
+                               m5=dict(avf_lim=1.0, prelax=1, amin=1e-6, pinf=[1.0, 0.0],
+                                       gamma=[2.0, 1.4], mu=[0.0, 0.0], rho0=[2.0, 1.0],
+                                       p0=[2.0, 1.0]),
+                               ic="m5 0 1 sphere 0.5 0.5 0.5 0.2 1"),
+    # hyperelastic solid below z = 0.25, liquid, gas bubble; a mixture slab whose solid
+    # fraction crosses AVF_LIM exercises the ghost-fluid fluxes and both velocity fixes
+    "m5_wall_gfm": rc.Case(trees=(2, 2, 2), level=3, steps=4, dt=1e-6, model=5,
+                           m5=dict(WALL, mix="2 0.25 0.375 0 0.4999999 1 5e6 0 0 -50"),
+                           ic=WALL_IC),
+    # the same on a 2:1 mesh refined around the bubble and wall
+    "m5_wall_amr": rc.Case(trees=(2, 2, 2), level=3, steps=3, dt=2e-8, model=5, m5=dict(WALL),
+                           refine="sphere 0.5 0.5 0.4 0.3 4 3", ic=WALL_IC),
+    "m5_wall_rk3_order1": rc.Case(trees=(2, 2, 2), level=3, steps=3, dt=2e-8, model=5,
+                                  m5=dict(WALL), rk_steps=3, order=1, ic=WALL_IC),
+}
+
+
 def config1_case() -> rc.Case:
     """Plain-method Sod problem of the 32^3 uniform forest: 4^3 trees at level 4, ideal
     gas, transmissive, MUSCL-HLLC, RK_STEPS 2, 100 steps.  The reference has no CFL
@@ -64,7 +94,11 @@ def save(name: str, c: rc.Case, keep_geom: bool) -> None:
         order=np.int32(c.order), gamma=np.float64(c.gamma), pinf=np.float64(c.pinf),
         root=final.root, level=final.level, adrs=final.adrs.astype(np.int8),
         S_init=init.S, S_final=final.S, ref_loop_seconds=np.float64(final.loop_seconds),
+        model=np.int32(c.model),
     )
+    if c.model == 5:
+        for key in ("avf_lim", "prelax", "amin", "pinf", "gamma", "mu"):
+            d["m5_" + key] = np.asarray(c.m5[key])
     if keep_geom:
         d.update(bc=final.bc.astype(np.int8), nn=final.nneig.astype(np.int8),
                  neigfc=final.neigfc.astype(np.int8), nb=final.nb, area=final.area,
@@ -80,6 +114,8 @@ def main() -> None:
         raise SystemExit("reference oracle could not be built")
     for name, (c, g) in CASES.items():
         save(name, c, g)
+    for name, c in M5_CASES.items():
+        save(name, c, True)
     save("m0_config1_sod32", config1_case(), False)
 
 

@@ -27,7 +27,7 @@ def run_gpu(mesh, S_aos, dt, steps, order=2, rk_steps=2, gamma=1.4, pinf=0.0):
     return out
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names(model=0))
 def test_gpu_matches_reference_fixture(name, built_lib):
     g = load_golden(name)
     m = mesh_from_golden(g)
