@@ -32,9 +32,12 @@ class FFVError(RuntimeError):
 class Params(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int32), ("nmaterials", ctypes.c_int32),
                 ("order", ctypes.c_int32), ("rk_steps", ctypes.c_int32),
-                ("precision", ctypes.c_int32), ("reserved0", ctypes.c_int32),
+                ("precision", ctypes.c_int32), ("prelax", ctypes.c_int32),
                 ("gamma", ctypes.c_double * FFV_MAX_MATERIALS),
-                ("pinf", ctypes.c_double * FFV_MAX_MATERIALS)]
+                ("pinf", ctypes.c_double * FFV_MAX_MATERIALS),
+                ("mu", ctypes.c_double * FFV_MAX_MATERIALS),
+                ("amin", ctypes.c_double), ("avf_lim", ctypes.c_double),
+                ("zerou", ctypes.c_int32 * 3), ("reserved1", ctypes.c_int32)]
 
 
 class ForestDesc(ctypes.Structure):

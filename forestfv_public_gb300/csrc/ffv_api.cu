@@ -7,6 +7,7 @@
 #include <new>
 
 #include "ffv_device.cuh"
+#include "ffv_m5.cuh"
 
 struct ffv_ctx {
   ffv_params p;
@@ -21,6 +22,11 @@ struct ffv_ctx {
   uint32_t *d_info;
   int32_t *d_nbr, *d_sub;
   double *d_S, *d_SN, *d_SF, *d_dt;
+  // model 5 only
+  double *d_Snew, *d_FF, *d_UF, *d_GF, *d_RHS;
+  uint8_t *d_flag;
+  int32_t *d_list, *d_bcount, *d_count;
+  M5Consts m5;
   unsigned int *d_status;
   unsigned long long *d_red;
   // pinned host scalars
@@ -48,9 +54,21 @@ void free_mesh_buffers(ffv_ctx *c) {
   cudaFree(c->d_S);
   cudaFree(c->d_SN);
   cudaFree(c->d_SF);
+  cudaFree(c->d_Snew);
+  cudaFree(c->d_FF);
+  cudaFree(c->d_UF);
+  cudaFree(c->d_GF);
+  cudaFree(c->d_RHS);
+  cudaFree(c->d_flag);
+  cudaFree(c->d_list);
+  cudaFree(c->d_bcount);
+  cudaFree(c->d_count);
   c->d_info = nullptr;
   c->d_nbr = c->d_sub = nullptr;
   c->d_S = c->d_SN = c->d_SF = nullptr;
+  c->d_Snew = c->d_FF = c->d_UF = c->d_GF = c->d_RHS = nullptr;
+  c->d_flag = nullptr;
+  c->d_list = c->d_bcount = c->d_count = nullptr;
   if (c->graph_valid) cudaGraphExecDestroy(c->graph);
   c->graph_valid = 0;
   c->have_mesh = c->have_state = 0;
@@ -62,15 +80,24 @@ unsigned status_to_err(unsigned st) {
   return FFV_OK;
 }
 
-int neq_of(const ffv_params &p) { return p.model == 0 ? 5 : -1; }
+int neq_of(const ffv_params &p) { return p.model == 0 ? 5 : ffv_m5_neq(p.nmaterials); }
 
 int launch_stage(ffv_ctx *c, int irk, cudaEvent_t *ev = nullptr) {
   ffv_m0_bufs b{c->d_S, c->d_SN, c->d_SF, c->d_dt, c->d_status};
   ffv_m0_consts k{c->p.gamma[0], c->p.pinf[0], c->p.order};
   if (irk == 0) {
-    CK(cudaMemcpyAsync(c->d_SN, c->d_S, sizeof(double) * 5 * c->n, cudaMemcpyDeviceToDevice,
+    CK(cudaMemcpyAsync(c->d_SN, c->d_S, sizeof(double) * c->neq * c->n, cudaMemcpyDeviceToDevice,
                        c->stream));
     return FFV_OK;
+  }
+  if (c->p.model == 5) {
+    ffv_m5_bufs mb{c->d_S,   c->d_SN,   c->d_Snew, c->d_SF,     c->d_FF,    c->d_UF,
+                   c->d_GF,  c->d_RHS,  c->d_dt,   c->d_flag,   c->d_list,  c->d_bcount,
+                   c->d_count, c->d_status};
+    if (ev) cudaEventRecord(ev[0], c->stream);
+    ffv_m5_fp64_stage(c->dm, c->geom, c->m5, mb, irk, c->stream);
+    if (ev) cudaEventRecord(ev[1], c->stream);
+    return cuda_rc(cudaGetLastError());
   }
   ffv_m0_fp64_stage(c->dm, c->geom, b, k, irk, c->stream, ev);
   return cuda_rc(cudaGetLastError());
@@ -189,7 +216,16 @@ const char *ffv_error_string(int code) {
 int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
   if (!out || !p) return FFV_ERR_ARG;
   *out = nullptr;
-  if (p->model != 0) return FFV_ERR_UNSUPPORTED;
+  if (p->model != 0 && p->model != 5) return FFV_ERR_UNSUPPORTED;
+  if (p->model == 5) {
+    if (p->nmaterials < 2 || p->nmaterials > 3) return FFV_ERR_UNSUPPORTED;
+    // PRELAX 2 reads relaxation arrays the reference never fills (F_pe.c:24 reads run->ar_R,
+    // run->t0_m, run->p0_m; m5_relaxationvec.c fills local arrays of the same names)
+    if (!(p->prelax == 3 || (p->prelax == 1 && p->nmaterials == 2))) return FFV_ERR_UNSUPPORTED;
+    int nsol = 0;
+    for (int i = 0; i < p->nmaterials; i++) nsol += p->mu[i] != 0.0;
+    if (nsol > 2) return FFV_ERR_UNSUPPORTED;
+  }
   if (p->order != 1 && p->order != 2) return FFV_ERR_ARG;
   if (p->rk_steps < 1 || p->rk_steps > 4) return FFV_ERR_ARG;
   if (p->precision != FFV_FP64 && p->precision != FFV_FP32_FLUX) return FFV_ERR_ARG;
@@ -204,6 +240,22 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
   c->p = *p;
   c->device = device;
   c->neq = neq_of(*p);
+  if (p->model == 5) {
+    M5Consts &k = c->m5;
+    k.nmat = p->nmaterials;
+    k.order = p->order;
+    k.prelax = p->prelax;
+    k.nsolids = 0;
+    for (int d = 0; d < 3; d++) k.zerou[d] = p->zerou[d];
+    for (int i = 0; i < FFV_MAX_MATERIALS; i++) {
+      k.gamma[i] = p->gamma[i];
+      k.pinf[i] = p->pinf[i];
+      k.mu[i] = p->mu[i];
+      if (i < p->nmaterials && p->mu[i] != 0.0) k.nsolids++;
+    }
+    k.amin = p->amin;
+    k.avf_lim = p->avf_lim;
+  }
   int rc = FFV_OK;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&c->d_dt, sizeof(double)) != cudaSuccess ||
@@ -245,6 +297,10 @@ int ffv_set_mesh(ffv_ctx *c, const ffv_mesh *m) {
   free_mesh_buffers(c);
   const int64_t n = m->n;
   const size_t nsub = (size_t)(m->nsub > 0 ? m->nsub : 1);
+  if (c->p.model == 5) {  // symmetry (bc 1) needs m5_hllc.c:56-85's central flux: not built
+    for (int s = 0; s < 6; s++)
+      if (m->desc.bc[s] == FFV_BC_SYMMETRY) return FFV_ERR_UNSUPPORTED;
+  }
   if (cudaMalloc(&c->d_info, sizeof(uint32_t) * n) != cudaSuccess ||
       cudaMalloc(&c->d_nbr, sizeof(int32_t) * 6 * n) != cudaSuccess ||
       cudaMalloc(&c->d_sub, sizeof(int32_t) * 4 * nsub) != cudaSuccess ||
@@ -253,6 +309,21 @@ int ffv_set_mesh(ffv_ctx *c, const ffv_mesh *m) {
       cudaMalloc(&c->d_SF, sizeof(double) * 6 * c->neq * n) != cudaSuccess) {
     free_mesh_buffers(c);
     return FFV_ERR_NOMEM;
+  }
+  if (c->p.model == 5) {
+    const int64_t nb = (n + 1023) / 1024;
+    if (cudaMalloc(&c->d_Snew, sizeof(double) * c->neq * n) != cudaSuccess ||
+        cudaMalloc(&c->d_FF, sizeof(double) * 6 * c->neq * n) != cudaSuccess ||
+        cudaMalloc(&c->d_UF, sizeof(double) * 18 * n) != cudaSuccess ||
+        cudaMalloc(&c->d_GF, sizeof(double) * 6 * n) != cudaSuccess ||
+        cudaMalloc(&c->d_RHS, sizeof(double) * c->neq * n) != cudaSuccess ||
+        cudaMalloc(&c->d_flag, n) != cudaSuccess ||
+        cudaMalloc(&c->d_list, sizeof(int32_t) * n) != cudaSuccess ||
+        cudaMalloc(&c->d_bcount, sizeof(int32_t) * nb) != cudaSuccess ||
+        cudaMalloc(&c->d_count, sizeof(int32_t)) != cudaSuccess) {
+      free_mesh_buffers(c);
+      return FFV_ERR_NOMEM;
+    }
   }
   // neighbour slots face-major on the device ([6][n]) for coalesced loads
   int32_t *nbr_t = (int32_t *)malloc(sizeof(int32_t) * 6 * n);
@@ -346,8 +417,12 @@ int ffv_cfl_dt(ffv_ctx *c, double cfl, double *dt_out) {
   if (!c->have_state) return FFV_ERR_STATE;
   CK(cudaSetDevice(c->device));
   CK(cudaMemsetAsync(c->d_red, 0xff, sizeof(unsigned long long), c->stream));
-  ffv_m0_consts k{c->p.gamma[0], c->p.pinf[0], c->p.order};
-  ffv_m0_cfl(c->dm, c->geom, c->d_S, k, c->d_red, c->stream);
+  if (c->p.model == 5) {
+    ffv_m5_cfl(c->dm, c->geom, c->m5, c->d_S, c->d_red, c->stream);
+  } else {
+    ffv_m0_consts k{c->p.gamma[0], c->p.pinf[0], c->p.order};
+    ffv_m0_cfl(c->dm, c->geom, c->d_S, k, c->d_red, c->stream);
+  }
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(c->h_red, c->d_red, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                      c->stream));
@@ -370,7 +445,7 @@ int ffv_profile_stage(ffv_ctx *c, int32_t irk, double dt, float *ms, int32_t max
                       int32_t *nkernels) {
   if (!c || !ms || !nkernels || irk < 1 || irk > 4) return FFV_ERR_ARG;
   if (!c->have_state) return FFV_ERR_STATE;
-  const int nk = ffv_m0_launches_per_stage(c->p.order);
+  const int nk = c->p.model == 5 ? 1 : ffv_m0_launches_per_stage(c->p.order);
   if (max_kernels < nk) return FFV_ERR_ARG;
   CK(cudaSetDevice(c->device));
   cudaEvent_t ev[8];
@@ -386,6 +461,7 @@ int ffv_profile_stage(ffv_ctx *c, int32_t irk, double dt, float *ms, int32_t max
 }
 
 const char *ffv_stage_kernel_name(const ffv_ctx *c, int32_t i) {
+  if (c && c->p.model == 5) return i == 0 ? "m5_stage (all kernels)" : "";
   return c ? ffv_m0_fp64_kernel_name(c->p.order, i) : "";
 }
 
@@ -397,7 +473,13 @@ int ffv_stream(ffv_ctx *c, void **stream) {
 
 int ffv_launches_per_step(const ffv_ctx *c, int32_t *n) {
   if (!c || !n) return FFV_ERR_ARG;
-  *n = c->p.rk_steps * ffv_m0_launches_per_stage(c->p.order);
+  if (c->p.model == 5) {
+    int t = 0;
+    for (int irk = 1; irk <= c->p.rk_steps; irk++) t += ffv_m5_launches_per_stage(c->m5, irk);
+    *n = t;
+  } else {
+    *n = c->p.rk_steps * ffv_m0_launches_per_stage(c->p.order);
+  }
   return FFV_OK;
 }
 

@@ -20,16 +20,24 @@ from .mesh import Mesh
 
 class Solver:
     def __init__(self, model: int = 0, order: int = 2, rk_steps: int = 2, gamma=(1.4,),
-                 pinf=(0.0,), precision: int = _lib.FFV_FP64, device: int = 0):
+                 pinf=(0.0,), precision: int = _lib.FFV_FP64, device: int = 0, mu=None,
+                 amin: float = 1e-6, avf_lim: float = 0.5, prelax: int = 3, zerou=(0, 0, 0)):
+        """model 0: gamma/pinf of the one material.  model 5: per-material gamma, pinf and
+        mu (shear modulus, 0 for fluids), AMIN, AVF_LIM, PRELAX (1 or 3), ZEROU masks."""
         L = _lib.lib()
         p = _lib.Params()
         p.model, p.nmaterials, p.order, p.rk_steps, p.precision = model, len(gamma), order, rk_steps, precision
+        p.prelax = prelax
         for i, g in enumerate(gamma):
             p.gamma[i] = g
         for i, q in enumerate(pinf):
             p.pinf[i] = q
+        for i, q in enumerate(mu or ()):
+            p.mu[i] = q
+        p.amin, p.avf_lim = amin, avf_lim
+        p.zerou[:] = tuple(zerou)
         self.params = p
-        self.neq = 5 if model == 0 else None
+        self.neq = 5 if model == 0 else 3 * len(gamma) + 12
         h = ctypes.c_void_p()
         _lib.check(L.ffv_create(ctypes.byref(h), ctypes.byref(p), device), "ffv_create")
         self._h = h

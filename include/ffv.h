@@ -65,14 +65,20 @@ extern "C" {
 
 /* Solver parameters: the reference's input globals for this path. */
 typedef struct ffv_params {
-  int32_t model;        /* MODEL: 0 (Euler, stiffened gas, m0_*) */
-  int32_t nmaterials;   /* NMATERIALS (1 for model 0) */
+  int32_t model;        /* MODEL: 0 (Euler, stiffened gas, m0_*) or 5 (m5_*: multi-material,
+                           hyperelastic solids, ghost-fluid coupling, pressure relaxation) */
+  int32_t nmaterials;   /* NMATERIALS (1 for model 0; 2 or 3 for model 5) */
   int32_t order;        /* ORDER: 1 (first order) or 2 (MUSCL, GRAD_SCHEME 1) */
   int32_t rk_steps;     /* RK_STEPS: 1..4; stage k uses the combination of RK.c case k */
   int32_t precision;    /* FFV_FP64 or FFV_FP32_FLUX */
-  int32_t reserved0;
+  int32_t prelax;       /* model 5: PRELAX 1 (two materials, closed form) or 3 (iterative) */
   double gamma[FFV_MAX_MATERIALS]; /* MATERGAMA */
   double pinf[FFV_MAX_MATERIALS];  /* MATERPINF */
+  double mu[FFV_MAX_MATERIALS];    /* model 5: MATERMUSH, shear modulus (0 for fluids) */
+  double amin;          /* model 5: AMIN, volume-fraction floor */
+  double avf_lim;       /* model 5: AVF_LIM, solid-fraction level of the ghost-fluid interface */
+  int32_t zerou[3];     /* model 5: ZEROU0..2 (freeze a velocity component, m5_RK.c:93-122) */
+  int32_t reserved1;
 } ffv_params;
 
 /* A Cartesian forest: ntrees[0] x ntrees[1] x ntrees[2] cubic hex trees of edge
