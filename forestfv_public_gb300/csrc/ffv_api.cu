@@ -32,6 +32,7 @@ struct ffv_ctx {
   // pinned host scalars
   unsigned int *h_status;
   unsigned long long *h_red;
+  const char *knames[16];  // kernel names of the last profiled stage
   // one captured time step
   cudaGraphExec_t graph;
   int graph_valid;
@@ -94,9 +95,7 @@ int launch_stage(ffv_ctx *c, int irk, cudaEvent_t *ev = nullptr) {
     ffv_m5_bufs mb{c->d_S,   c->d_SN,   c->d_Snew, c->d_SF,     c->d_FF,    c->d_UF,
                    c->d_GF,  c->d_RHS,  c->d_dt,   c->d_flag,   c->d_list,  c->d_bcount,
                    c->d_count, c->d_status};
-    if (ev) cudaEventRecord(ev[0], c->stream);
-    ffv_m5_fp64_stage(c->dm, c->geom, c->m5, mb, irk, c->stream);
-    if (ev) cudaEventRecord(ev[1], c->stream);
+    ffv_m5_fp64_stage(c->dm, c->geom, c->m5, mb, irk, c->stream, ev, c->knames);
     return cuda_rc(cudaGetLastError());
   }
   ffv_m0_fp64_stage(c->dm, c->geom, b, k, irk, c->stream, ev);
@@ -445,10 +444,11 @@ int ffv_profile_stage(ffv_ctx *c, int32_t irk, double dt, float *ms, int32_t max
                       int32_t *nkernels) {
   if (!c || !ms || !nkernels || irk < 1 || irk > 4) return FFV_ERR_ARG;
   if (!c->have_state) return FFV_ERR_STATE;
-  const int nk = c->p.model == 5 ? 1 : ffv_m0_launches_per_stage(c->p.order);
+  const int nk = c->p.model == 5 ? ffv_m5_launches_per_stage(c->m5, irk)
+                                 : ffv_m0_launches_per_stage(c->p.order);
   if (max_kernels < nk) return FFV_ERR_ARG;
   CK(cudaSetDevice(c->device));
-  cudaEvent_t ev[8];
+  cudaEvent_t ev[17];
   for (int i = 0; i <= nk; i++) CK(cudaEventCreate(&ev[i]));
   int rc = queue_dt(c, dt);
   if (rc == FFV_OK) rc = launch_stage(c, irk, ev);
@@ -461,7 +461,7 @@ int ffv_profile_stage(ffv_ctx *c, int32_t irk, double dt, float *ms, int32_t max
 }
 
 const char *ffv_stage_kernel_name(const ffv_ctx *c, int32_t i) {
-  if (c && c->p.model == 5) return i == 0 ? "m5_stage (all kernels)" : "";
+  if (c && c->p.model == 5) return (i >= 0 && i < 16 && c->knames[i]) ? c->knames[i] : "";
   return c ? ffv_m0_fp64_kernel_name(c->p.order, i) : "";
 }
 

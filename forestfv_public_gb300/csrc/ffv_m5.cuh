@@ -20,8 +20,11 @@ struct ffv_m5_bufs {
 };
 
 int ffv_m5_neq(int nmat);
+// ev (nullable): an event before the first and after every kernel; names[i] receives
+// kernel i's name
 void ffv_m5_fp64_stage(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
-                       const ffv_m5_bufs &b, int irk, cudaStream_t st);
+                       const ffv_m5_bufs &b, int irk, cudaStream_t st, cudaEvent_t *ev,
+                       const char **names);
 int ffv_m5_launches_per_stage(const M5Consts &k, int irk);
 void ffv_m5_cfl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
                 unsigned long long *d_out, cudaStream_t st);

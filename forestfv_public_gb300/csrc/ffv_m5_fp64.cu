@@ -9,8 +9,10 @@
 // One stage:
 //   m5_recon_face   (cell, face)  MUSCL face state + face-state pressure relaxation
 //                                  (m5_faceinterp_V1 / m5_reconctruct_V1 / m5_relaxationvec)
-//   m5_face_flux    (cell, face)  HLLC or ghost-fluid HLLC per face or subface, with the
-//                                  reference's flux reuse on 1:1 faces (m5_residual.c:59-173)
+//   m5_face_flux    (cell, face)  HLLC or ghost-fluid HLLC per face or subface; a 1:1 face
+//                                  is evaluated once, by the cell first in leaf order, and
+//                                  the other takes its negative (the reference's flux
+//                                  reuse, m5_residual.c:59-173)
 //   m5_cell_update  (cell)        residual sum + non-conservative terms (m5_residual.c:175-215),
 //                                  RK stage (m5_RK.c), positivity and ZEROU masks
 //   compaction + m5_gfm_seq       cells whose solid fraction crosses AVF_LIM in stage 1, in
@@ -776,7 +778,7 @@ template <int N, int F>
 __device__ void face_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
                           const double *__restrict__ S, const double *__restrict__ SF, int64_t c,
                           uint32_t info, double *ff, double uf[3], double &gfm_face,
-                          unsigned &st) {
+                          unsigned &st, bool &owner) {
   using C = K5<N>;
   constexpr int FO = fr_opp(F);
   const uint32_t kind = ffv_face_kind(info, F);
@@ -788,28 +790,12 @@ __device__ void face_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts 
   gfm_face = 0.0;
   Sol<N> L, R;
   load_state<N>(S, m.n, c, Sc);
-  if (kind == FFV_FK_SAME) {
-    const int64_t o = m.nbr[(int64_t)F * m.n + c];
-    load_state<N>(S, m.n, o, So);
-    if (o < c) {
-      // evaluated by the neighbour (first in leaf order) with its own state on the left;
-      // this cell takes the negative flux and face velocity, and no ghost-fluid flag
-      double t[C::NEQ], ut[3];
-#pragma unroll
-      for (int iv = 0; iv < C::NEQ; iv++) t[iv] = 0.0;
-      if (k.order == 2) load_face_state<N>(SF, m.n, FO, o, U);
-      make_sol<N>(k, k.order == 2 ? U : So, So, k.order == 2, L);
-      if (k.order == 2) load_face_state<N>(SF, m.n, F, c, U);
-      make_sol<N>(k, k.order == 2 ? U : Sc, Sc, k.order == 2, R);
-      const bool gfm = L.phi0 * R.phi0 < 0.0;
-      st |= hllc_acc<FO, N>(k, L, R, 0, gfm, g.area[l], t, ut);
-#pragma unroll
-      for (int iv = 0; iv < C::NEQ; iv++) ff[iv] = -t[iv];
-      uf[0] = -(ut[0] / 1.0);
-      uf[1] = -(ut[1] / 1.0);
-      uf[2] = -(ut[2] / 1.0);
-      return;
-    }
+  if (kind == FFV_FK_SAME && m.nbr[(int64_t)F * m.n + c] < c) {
+    // 1:1 face whose neighbour comes first in leaf order: the neighbour's thread evaluates
+    // it (face F^1 of the neighbour) and m5_cell_update takes the negative, as the
+    // reference's flux reuse does (m5_residual.c:80-99); no ghost-fluid flag here
+    owner = false;
+    return;
   }
   if (k.order == 2) load_face_state<N>(SF, m.n, F, c, U);
   make_sol<N>(k, k.order == 2 ? U : Sc, Sc, k.order == 2, L);
@@ -854,20 +840,23 @@ __global__ void __launch_bounds__(128) m5_face_flux(ffv_dmesh m, ffv_geom g, M5C
   const int f = (int)(t / m.n);
   const int64_t c = t - (int64_t)f * m.n;
   const uint32_t info = m.info[c];
-  double ff[C::NEQ], uf[3], gf;
+  double ff[C::NEQ], uf[3], gf = 0.0;
   unsigned st = 0;
+  bool owner = true;
   switch (f) {
-    case 0: face_flux<N, 0>(m, g, k, S, SF, c, info, ff, uf, gf, st); break;
-    case 1: face_flux<N, 1>(m, g, k, S, SF, c, info, ff, uf, gf, st); break;
-    case 2: face_flux<N, 2>(m, g, k, S, SF, c, info, ff, uf, gf, st); break;
-    case 3: face_flux<N, 3>(m, g, k, S, SF, c, info, ff, uf, gf, st); break;
-    case 4: face_flux<N, 4>(m, g, k, S, SF, c, info, ff, uf, gf, st); break;
-    default: face_flux<N, 5>(m, g, k, S, SF, c, info, ff, uf, gf, st); break;
+    case 0: face_flux<N, 0>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 1: face_flux<N, 1>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 2: face_flux<N, 2>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 3: face_flux<N, 3>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 4: face_flux<N, 4>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    default: face_flux<N, 5>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
   }
+  if (owner) {
 #pragma unroll
-  for (int iv = 0; iv < C::NEQ; iv++) FF[((int64_t)f * C::NEQ + iv) * m.n + c] = ff[iv];
+    for (int iv = 0; iv < C::NEQ; iv++) FF[((int64_t)f * C::NEQ + iv) * m.n + c] = ff[iv];
 #pragma unroll
-  for (int d = 0; d < 3; d++) UF[((int64_t)f * 3 + d) * m.n + c] = uf[d];
+    for (int d = 0; d < 3; d++) UF[((int64_t)f * 3 + d) * m.n + c] = uf[d];
+  }
   GF[(int64_t)f * m.n + c] = gf;
   if (st) atomicOr(status, st);
 }
@@ -965,11 +954,26 @@ __global__ void __launch_bounds__(128) m5_cell_update(ffv_dmesh m, ffv_geom g, M
   for (int iv = 0; iv < C::NEQ; iv++) rhs[iv] = 0.0;
 #define FACE(F)                                                                          \
   {                                                                                      \
-    _Pragma("unroll") for (int iv = 0; iv < C::NEQ; iv++) rhs[iv] +=                     \
-        FF[((int64_t)F * C::NEQ + iv) * m.n + c];                                        \
-    nonconservative<N, F>(g, Cs, ast, info, l, UF[((int64_t)F * 3 + 0) * m.n + c],       \
-                          UF[((int64_t)F * 3 + 1) * m.n + c],                            \
-                          UF[((int64_t)F * 3 + 2) * m.n + c], rhs);                      \
+    int64_t fc = c;                                                                      \
+    int ff = F;                                                                          \
+    double sg = 1.0;                                                                     \
+    if (ffv_face_kind(info, F) == FFV_FK_SAME) {                                         \
+      const int64_t o = m.nbr[(int64_t)F * m.n + c];                                     \
+      if (o < c) {                                                                       \
+        fc = o;                                                                          \
+        ff = fr_opp(F);                                                                  \
+        sg = -1.0;                                                                       \
+      }                                                                                  \
+    }                                                                                    \
+    _Pragma("unroll") for (int iv = 0; iv < C::NEQ; iv++) {                              \
+      const double x = FF[((int64_t)ff * C::NEQ + iv) * m.n + fc];                       \
+      rhs[iv] += sg < 0.0 ? -x : x;                                                      \
+    }                                                                                    \
+    const double u0 = UF[((int64_t)ff * 3 + 0) * m.n + fc];                              \
+    const double u1 = UF[((int64_t)ff * 3 + 1) * m.n + fc];                              \
+    const double u2 = UF[((int64_t)ff * 3 + 2) * m.n + fc];                              \
+    nonconservative<N, F>(g, Cs, ast, info, l, sg < 0.0 ? -u0 : u0, sg < 0.0 ? -u1 : u1, \
+                          sg < 0.0 ? -u2 : u2, rhs);                                     \
   }
   FACE(0) FACE(1) FACE(2) FACE(3) FACE(4) FACE(5)
 #undef FACE
@@ -1327,38 +1331,73 @@ void ffv_m5_cfl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const 
 
 int ffv_m5_neq(int nmat) { return 3 * nmat + 12; }
 
+// kernel names in launch order, for ffv_profile_stage
+static const char *k_names[] = {"m5_recon_face", "m5_face_flux",  "m5_cell_update",
+                                "flag_count",    "flag_scan",     "flag_scatter",
+                                "m5_gfm_seq",    "m5_relax_cell", "flag_count",
+                                "flag_scan",     "flag_scatter",  "m5_gfm_seq(relax)"};
+
+struct Rec {
+  cudaEvent_t *ev;
+  int i;
+  const char **names;
+  cudaStream_t st;
+  void operator()(const char *name) {
+    if (ev) {
+      names[i] = name;
+      cudaEventRecord(ev[++i], st);
+    }
+  }
+};
+
 template <int N>
 static void stage_impl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
-                       const ffv_m5_bufs &b, int irk, cudaStream_t st) {
-  using C = K5<N>;
+                       const ffv_m5_bufs &b, int irk, cudaStream_t st, cudaEvent_t *ev,
+                       const char **names) {
   const int tpb = 128;
   const unsigned gf = (unsigned)((6 * m.n + tpb - 1) / tpb), gc = (unsigned)((m.n + tpb - 1) / tpb);
   const unsigned nb = (unsigned)((m.n + CB - 1) / CB);
-  if (k.order == 2) m5_recon_face<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.status);
+  Rec rec{ev, 0, names, st};
+  if (ev) cudaEventRecord(ev[0], st);
+  if (k.order == 2) {
+    m5_recon_face<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.status);
+    rec(k_names[0]);
+  }
   m5_face_flux<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.FF, b.UF, b.GF, b.status);
+  rec(k_names[1]);
   m5_cell_update<N><<<gc, tpb, 0, st>>>(m, g, k, b.S, b.SN, b.FF, b.UF, b.RHS, b.Snew, b.flag,
                                         b.dt, irk, b.status);
+  rec(k_names[2]);
   if (irk == 1) {
     flag_count<<<nb, CB, 0, st>>>(m.n, b.flag, b.bcount);
+    rec(k_names[3]);
     flag_scan<<<1, CB, 0, st>>>((int)nb, b.bcount, b.count);
+    rec(k_names[4]);
     flag_scatter<<<nb, CB, 0, st>>>(m.n, b.flag, b.bcount, b.list);
+    rec(k_names[5]);
     m5_gfm_seq<N><<<1, 32, 0, st>>>(m, g, k, b.list, b.count, b.S, b.Snew, b.SN, b.RHS, b.GF,
                                     b.dt, 0);
+    rec(k_names[6]);
   }
   m5_relax_cell<N><<<gc, tpb, 0, st>>>(m.n, k, b.Snew, b.S, b.flag, b.status);
+  rec(k_names[7]);
   flag_count<<<nb, CB, 0, st>>>(m.n, b.flag, b.bcount);
+  rec(k_names[8]);
   flag_scan<<<1, CB, 0, st>>>((int)nb, b.bcount, b.count);
+  rec(k_names[9]);
   flag_scatter<<<nb, CB, 0, st>>>(m.n, b.flag, b.bcount, b.list);
+  rec(k_names[10]);
   // relaxed states are in S; a later neighbour is still unrelaxed (Snew)
   m5_gfm_seq<N><<<1, 32, 0, st>>>(m, g, k, b.list, b.count, b.Snew, b.S, b.SN, b.RHS, b.GF,
                                   b.dt, 1);
-  (void)C::NEQ;
+  rec(k_names[11]);
 }
 
 void ffv_m5_fp64_stage(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
-                       const ffv_m5_bufs &b, int irk, cudaStream_t st) {
-  if (k.nmat == 2) stage_impl<2>(m, g, k, b, irk, st);
-  else stage_impl<3>(m, g, k, b, irk, st);
+                       const ffv_m5_bufs &b, int irk, cudaStream_t st, cudaEvent_t *ev,
+                       const char **names) {
+  if (k.nmat == 2) stage_impl<2>(m, g, k, b, irk, st, ev, names);
+  else stage_impl<3>(m, g, k, b, irk, st, ev, names);
 }
 
 int ffv_m5_launches_per_stage(const M5Consts &k, int irk) {

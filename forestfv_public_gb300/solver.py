@@ -86,12 +86,16 @@ class Solver:
 
     def profile_stage(self, irk: int, dt: float) -> dict:
         """Per-kernel durations (ms) of one stage, CUDA events on the solver's stream."""
-        ms = np.zeros(8, dtype=np.float32)
+        ms = np.zeros(16, dtype=np.float32)
         nk = ctypes.c_int32()
         L = _lib.lib()
-        _lib.check(L.ffv_profile_stage(self._h, irk, dt, ms.ctypes.data, 8, ctypes.byref(nk)),
+        _lib.check(L.ffv_profile_stage(self._h, irk, dt, ms.ctypes.data, 16, ctypes.byref(nk)),
                    "ffv_profile_stage")
-        return {L.ffv_stage_kernel_name(self._h, i).decode(): float(ms[i]) for i in range(nk.value)}
+        out = {}
+        for i in range(nk.value):
+            name = L.ffv_stage_kernel_name(self._h, i).decode()
+            out[name] = out.get(name, 0.0) + float(ms[i])
+        return out
 
     def stream_handle(self) -> int:
         p = ctypes.c_void_p()

@@ -1,0 +1,111 @@
+"""Synthetic workloads of the benchmark configurations (meshes and initial states).
+
+Everything is generated from fixed seeds; no external data.  Levels follow the reference:
+trees are level 1, a leaf at level l has 2**(l-1) cells per tree edge.  With the 2^3-tree
+unit cube used here, "level L" of the configurations (2**L cells per edge) is reference
+level L.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .mesh import Leaves, Mesh
+
+# corner k of a child sits at (x, y, z) = (bit1(k), bit0(k), bit2(k))
+_OFF = np.array([[(k >> 1) & 1, k & 1, (k >> 2) & 1] for k in range(8)], dtype=np.int64)
+
+
+def refine_to_target(ntrees, lmin: int, lmax: int, target) -> Leaves:
+    """Top-down octree refinement of every tree from level lmin: a cell of level l is
+    split while target(centres, h) > l (vectorised over cells).  `target` must fall off
+    by at most one level per two cells of the coarser level so that the result is 2:1
+    balanced (ffv_mesh_build checks it)."""
+    T = np.asarray(ntrees, dtype=np.int64)
+    edge = 1.0 / T.max()
+    e = 1 << (lmin - 1)
+    g = np.stack(np.meshgrid(*[np.arange(t * e) for t in T], indexing="ij"), -1).reshape(-1, 3)
+    out_g, out_l = [], []
+    for l in range(lmin, lmax + 1):
+        h = edge / (1 << (l - 1))
+        cen = (g + 0.5) * h
+        split = target(cen, h) > l if l < lmax else np.zeros(len(g), bool)
+        out_g.append(g[~split])
+        out_l.append(np.full((~split).sum(), l, np.int32))
+        g = (2 * g[split][:, None, :] + _OFF[None, :, :]).reshape(-1, 3)
+    gg = np.concatenate(out_g)
+    ll = np.concatenate(out_l)
+    per_tree = (1 << (ll - 1)).astype(np.int64)
+    tree = gg // per_tree[:, None]
+    cell = gg - tree * per_tree[:, None]
+    return Leaves(tree.astype(np.int32), ll, cell.astype(np.int32))
+
+
+BUBBLE = dict(gamma=(4.4, 1.4), pinf=(6e8, 0.0), rho=(1000.0, 1.0), p=(5e6, 1e5), mu=(0.0, 0.0),
+              amin=1e-6)
+
+
+def bubble_config2(lmin: int = 4, lmax: int = 8, band_cells: float = 22.0, seed: int = 20261203,
+                   radius: float = 0.1):
+    """Two-phase gas bubble collapse in liquid (the second configuration): liquid
+    (stiffened gas, gamma 4.4, p_inf 6e8, rho 1000, p 5e6) around a gas sphere (gamma 1.4,
+    rho 1, p 1e5) of radius 0.1 at the centre, interface smoothed over two finest cells
+    with tanh in volume fraction, radius perturbed by seeded harmonics l <= 8 of relative
+    amplitude 1e-3; 2^3 trees, levels lmin..lmax refined around the interface.
+    Returns (Mesh, S [neq, n], params)."""
+    c0 = np.array([0.5, 0.5, 0.5])
+    hmin = 0.5 / (1 << (lmax - 1))
+    coeff_rng = np.random.default_rng(seed + 1)
+    coef = [(l, m, coeff_rng.uniform(-1e-3, 1e-3)) for l in range(1, 9) for m in range(-l, l + 1)]
+
+    def radius_at(x):
+        d = x - c0
+        r = np.linalg.norm(d, axis=1)
+        theta = np.arccos(np.clip(d[:, 2] / np.maximum(r, 1e-300), -1, 1))
+        phi = np.arctan2(d[:, 1], d[:, 0])
+        from scipy.special import sph_harm_y
+        s = np.zeros_like(r)
+        for l, m, a in coef:
+            y = sph_harm_y(l, abs(m), theta, phi)
+            yr = np.sqrt(2) * (y.imag if m < 0 else y.real) if m != 0 else y.real
+            s += a * yr
+        return r, radius * (1.0 + s)
+
+    def target(cen, h):
+        # the refinement band follows the unperturbed sphere (the perturbation is 1e-3 R)
+        r = np.linalg.norm(cen - c0, axis=1)
+        d = np.abs(r - radius) - 0.8660254 * h
+        lev = lmax - np.floor(np.maximum(d, 0.0) / (band_cells * hmin * 2.0)).astype(np.int64)
+        return np.maximum(lev, lmin)
+
+    leaves = refine_to_target((2, 2, 2), lmin, lmax, target)
+    mesh = Mesh((2, 2, 2), leaves)
+    x = mesh.centroids()
+    w = 2.0 * hmin
+    r = np.linalg.norm(x - c0, axis=1)
+    R = np.full_like(r, radius)
+    near = np.abs(r - radius) < 20.0 * w  # the tanh profile is saturated beyond this
+    r[near], R[near] = radius_at(x[near])
+    a_gas = 0.5 * (1.0 - np.tanh((r - R) / w))
+    S = mixture_state(BUBBLE, a_gas)
+    return mesh, S, dict(BUBBLE)
+
+
+def mixture_state(mat: dict, a_gas: np.ndarray) -> np.ndarray:
+    """Two-material state [neq=18, n] at rest: material 0 liquid, 1 gas, each at its own
+    initial pressure weighted by volume fraction (pressure equilibrium within a cell)."""
+    amin = mat["amin"]
+    a1 = np.clip(a_gas, amin, 1.0 - amin)
+    a0 = 1.0 - a1
+    p = a0 * mat["p"][0] + a1 * mat["p"][1]
+    n = len(a_gas)
+    N = 2
+    S = np.zeros((3 * N + 12, n))
+    E = np.zeros(n)
+    for k, a in enumerate((a0, a1)):
+        S[k] = a * mat["rho"][k]
+        are = a * (p + mat["gamma"][k] * mat["pinf"][k]) / (mat["gamma"][k] - 1.0)
+        S[2 * N + 3 + k] = are
+        E += are
+    S[N + 3] = E
+    S[N + 4] = a0
+    return S
