@@ -71,11 +71,14 @@ def _bubble_solver_kwargs(p):
                 amin=p["amin"], avf_lim=1.0, prelax=3)
 
 
-def wl_config2(small: bool = False):
+def wl_config2(small: bool = False, medium: bool = False):
     from forestfv_public_gb300 import workloads as W
     if small:  # CPU sample: same physics, levels 4..6
         mesh, S0, p = W.bubble_config2(lmin=4, lmax=6, band_cells=2.0)
         hmin = 0.5 / (1 << 5)
+    elif medium:  # profiler captures: levels 4..7, 0.36 M cells
+        mesh, S0, p = W.bubble_config2(lmin=4, lmax=7, band_cells=12.0)
+        hmin = 0.5 / (1 << 6)
     else:
         mesh, S0, p = W.bubble_config2()
         hmin = 0.5 / (1 << 7)
@@ -109,7 +112,14 @@ def wl_config1(small: bool = False):
     return mesh, S0, float(dt), cfg, dict(model=0), alg, True
 
 
-WORKLOADS = {"config2": wl_config2, "config1": wl_config1}
+def wl_config2m(small: bool = False):
+    """config2 physics on a 0.36 M-cell mesh (levels 4-7): the size profiler captures use."""
+    out = wl_config2(small=small, medium=not small)
+    out[3]["workload"] = out[3]["workload"].replace("levels 5-8", "levels 4-7 (medium size)")
+    return out
+
+
+WORKLOADS = {"config2": wl_config2, "config1": wl_config1, "config2m": wl_config2m}
 
 
 # ------------------------------------------------------------------------------ helpers

@@ -549,10 +549,15 @@ __device__ unsigned relaxationvec(const M5Consts &k, double *V) {
         p_relaxed += avf[iv] * pkinit[iv];
       }
       int iter = 0;
-      double F = 1.0e-9, dF = 1.0e9;
+      double F = 1.0e-9, dF = 1.0e9, p_prev = NAN;
 #pragma unroll
       for (int iv = 0; iv < N; ++iv) rhoKs[iv] = 0.0;
-      // the reference's own iteration cap (m5_relaxationvec.c:458) bounds this loop
+      // the reference's own iteration cap (m5_relaxationvec.c:458) bounds this loop.  An
+      // iterate that repeats bitwise is a fixed point: F, dF and rhoKs repeat with it, so
+      // the remaining iterations up to the cap would recompute the same values -- leaving
+      // there gives exactly the reference's result (most non-converging face states of a
+      // stiff two-phase interface reach such a point within a few iterations and would
+      // otherwise spin to the cap).
       while ((fabs(F) > 1.0e-12) && (iter < 500)) {
         p_relaxed = p_relaxed - F / dF;
         iter = iter + 1;
@@ -576,6 +581,8 @@ __device__ unsigned relaxationvec(const M5Consts &k, double *V) {
           st |= FFV_ST_NAN;
           break;
         }
+        if (p_relaxed == p_prev) break;
+        p_prev = p_relaxed;
       }
 #pragma unroll
       for (int iv = 0; iv < N; ++iv)
