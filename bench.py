@@ -184,17 +184,18 @@ def peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str, cells: int):
-    """DRAM bytes per launch from the committed ncu summary (bytes per cell x cells)."""
+def ncu_summary(kernel: str, cells: int):
+    """(DRAM bytes per launch, FP64-pipe % busy) of a kernel from the committed ncu summary
+    (bytes per cell x cells); None where the kernel has no capture."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     try:
         for ln in open(p):
             t = ln.split()
             if len(t) >= 2 and not ln.startswith("#") and t[0] == kernel:
-                return float(t[1]) * cells
+                return float(t[1]) * cells, (float(t[2]) if len(t) > 2 else None)
     except OSError:
         pass
-    return None
+    return None, None
 
 
 _CPU_CACHE = {}
@@ -332,8 +333,10 @@ def run_ours(args) -> None:
     alg = alg_bytes.get(dom, 0) * mesh.n
     achieved = alg / (mean_ms[dom] / 1e3) / 1e9
     step_ms = sum(mean_ms.values())
+    traffic, fp64_pct = ncu_summary(dom, mesh.n)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": ncu_traffic(dom, mesh.n), "kernel": dom,
+                "frac": achieved / peak, "traffic": traffic, "kernel": dom,
+                "fp64_pipe_busy_pct_ncu": fp64_pct,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst)",
                 "kernel_mean_ms_per_stage": mean_ms,
                 "kernel_share": {k: v / step_ms for k, v in mean_ms.items()},
