@@ -208,6 +208,7 @@ const char *ffv_error_string(int code) {
     case FFV_ERR_UNSUPPORTED: return "unsupported option";
     case FFV_ERR_NOMEM: return "out of memory";
     case FFV_ERR_STATE: return "call out of order";
+    case FFV_ERR_TOO_LARGE: return "mesh larger than the no-allocation scratch";
     default: return "unknown error";
   }
 }

@@ -46,6 +46,7 @@ extern "C" {
 #define FFV_ERR_UNSUPPORTED 8  /* option outside what this build implements              */
 #define FFV_ERR_NOMEM 9        /* host or device allocation failed                       */
 #define FFV_ERR_STATE 10       /* call out of order (e.g. step before mesh/state upload) */
+#define FFV_ERR_TOO_LARGE 11   /* mesh larger than the fixed scratch of ffv_step_noalloc */
 
 #define FFV_MAX_MATERIALS 8
 #define FFV_MAX_NEQ 32
@@ -155,6 +156,29 @@ const char *ffv_stage_kernel_name(const ffv_ctx *ctx, int32_t i);
 int ffv_launches_per_step(const ffv_ctx *ctx, int32_t *n);
 
 const char *ffv_error_string(int code);
+
+/* No-allocation model-0 step -- no counterpart in the reference.
+ * For callers that cannot allocate device memory: a plugin or library that is handed
+ * device buffers by a host application or framework which owns all allocation (its own
+ * arena or caching allocator, a fixed memory budget), or a loop that must not call
+ * cudaMalloc/cudaFree because they synchronise the device.  Advances the model-0 FP64
+ * state d_S (device memory of the current device, SoA [5][ncells], updated in place) by
+ * nsteps time steps of p->rk_steps stages on `stream` (a cudaStream_t; NULL = the legacy
+ * default stream), with the same kernels and results as ffv_step, then waits for the
+ * stream and returns the first error the device recorded.  It allocates nothing, on the
+ * device or the host: the face tables of `m`, the RK copy and the face states live in one
+ * fixed device array of FFV_NOALLOC_SCRATCH_BYTES inside this library, which every GPU
+ * that loads the library holds until the process exits.  Meshes of more than
+ * FFV_NOALLOC_MAX_CELLS cells are rejected with FFV_ERR_TOO_LARGE; models other than 0
+ * and precisions other than FFV_FP64 with FFV_ERR_UNSUPPORTED.  All calls on a device
+ * share the array and it keeps the last call's contents (each call rewrites what it
+ * reads and clears its status word first); calls whose work overlaps on the GPU race on
+ * it.  The first call on a device looks up the array's address (cudaGetSymbolAddress) and
+ * should come before any stream capture on that device. */
+#define FFV_NOALLOC_MAX_CELLS 65536
+#define FFV_NOALLOC_SCRATCH_BYTES 21758464
+int ffv_step_noalloc(const ffv_mesh *m, const ffv_params *p, double *d_S, double dt,
+                     int32_t nsteps, void *stream);
 
 #ifdef __cplusplus
 }
