@@ -269,6 +269,66 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+FP32_PERTURBATION = 1e-7
+
+
+def measure_fp32_form(mesh, S0, dt, kw, args, dev, fp64_solver) -> dict:
+    """The FP32-flux form (precision FFV_FP32_FLUX) on the same workload: throughput with
+    CUDA events on its stream, per-kernel times, and its error against the FP64 form after
+    `args.steps` steps next to the FP64 form's own spread when its initial state is
+    perturbed by FP32_PERTURBATION (relative, seeded): the sensitivity floor that any
+    re-rounded arithmetic meets on this problem."""
+    import torch
+
+    from forestfv_public_gb300 import Solver
+    from forestfv_public_gb300.fields import error_report
+    s32 = Solver(device=dev.index, precision=1, **kw)
+    s32.set_mesh(mesh)
+    s32.upload_state(S0)
+    stream = torch.cuda.ExternalStream(s32.stream_handle(), device=dev)
+    s32.step(dt, args.warmup)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    torch.cuda.synchronize(dev)
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            ev[k][0].record(stream)
+        s32.step_async(dt, 1)
+        ev[k][1].record(stream)
+    s32.sync()
+    torch.cuda.synchronize(dev)
+    t_ms = sum(a.elapsed_time(b) for a, b in ev)
+    per_kernel = {}
+    for _ in range(3):
+        for irk in (1, 2):
+            for name, ms in s32.profile_stage(irk, dt).items():
+                per_kernel.setdefault(name, []).append(ms)
+    mean_ms = {k: sum(v) / len(v) for k, v in per_kernel.items()}
+
+    def advance(solver, S):
+        solver.upload_state(S)
+        solver.step(dt, args.steps)
+        return solver.download_state()
+
+    mu = kw.get("mu")
+    solid = 0 if mu is not None and mu[0] != 0.0 else None
+    ref = advance(fp64_solver, S0)
+    err = error_report(advance(s32, S0), ref, kw["gamma"], kw["pinf"], mu, kw["amin"], solid)
+    rng = np.random.default_rng(20261203)
+    Sp = S0 * (1.0 + FP32_PERTURBATION * rng.uniform(-1.0, 1.0, S0.shape))
+    floor = error_report(advance(fp64_solver, Sp), ref, kw["gamma"], kw["pinf"], mu, kw["amin"],
+                         solid)
+    s32.close()
+    return {"value": mesh.n * args.steps / (t_ms / 1e3), "unit": UNIT,
+            "ms_per_step": t_ms / args.steps, "kernel_mean_ms_per_stage": mean_ms,
+            "error_vs_fp64": err, "error_steps": args.steps,
+            "fp64_sensitivity_floor": {"perturbation": FP32_PERTURBATION, **floor},
+            "note": "error of the FP32-flux form against the FP64 form after error_steps steps, "
+                    "beside the FP64 form's own change when its initial state is perturbed by "
+                    "1e-7 relative: the reference's model-5 scheme amplifies rounding-level "
+                    "differences, so the FP32 form is judged against that floor"}
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -366,6 +426,10 @@ def run_ours(args) -> None:
             cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
                    "sample": f"{csteps} steps of a {n}-cell mesh of the same problem, oracle C "
                              "restatement of the reference algorithm"}
+        fp32 = None
+        if world == 1 and kw.get("model", 0) == 5 and not args.no_fp32_form:
+            fp32 = measure_fp32_form(mesh, S0, dt, kw, args, dev, solver)
+            fp32["speedup_vs_fp64"] = fp32["value"] / value
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
@@ -374,6 +438,8 @@ def run_ours(args) -> None:
             "clocks": clock_info,
             "gpu_launches": solver.launches_per_step() * args.steps,
         }
+        if fp32 is not None:
+            line["fp32_flux_form"] = fp32
         print(json.dumps(line), flush=True)
     solver.close()
     if world > 1:
@@ -388,6 +454,8 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--workload", default="config2", choices=tuple(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-fp32-form", action="store_true",
+                    help="skip the FP32-flux form's throughput and error report")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

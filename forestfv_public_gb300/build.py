@@ -29,6 +29,7 @@ SOURCES = {
     "ffv_api.cu": [],
     "ffv_m0_fp64.cu": ["--fmad=false"],
     "ffv_m5_fp64.cu": ["--fmad=false"],
+    "ffv_m5_fp32.cu": [],
     "ffv_noalloc.cu": [],
 }
 

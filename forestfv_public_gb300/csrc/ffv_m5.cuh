@@ -7,6 +7,7 @@
 
 struct M5Consts {
   int nmat, order, prelax, nsolids;
+  int precision;  // FFV_FP64 or FFV_FP32_FLUX
   int zerou[3];
   double gamma[FFV_MAX_MATERIALS], pinf[FFV_MAX_MATERIALS], mu[FFV_MAX_MATERIALS];
   double amin, avf_lim;
@@ -26,5 +27,19 @@ void ffv_m5_fp64_stage(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
                        const ffv_m5_bufs &b, int irk, cudaStream_t st, cudaEvent_t *ev,
                        const char **names);
 int ffv_m5_launches_per_stage(const M5Consts &k, int irk);
+
+// FP32-flux form (ffv_m5_fp32.cu): face states and face fluxes in FP32.
+//   SFf: [6][neq + nmat][n] float -- the reconstructed, relaxed face state (conserved
+//        variables) followed by each material's pressure, recovered in FP64
+//   FFf: [6][neq][n] float face fluxes (area-weighted), UFf: [6][3][n] float face velocity
+void ffv_m5f_recon(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
+                   float *SFf, unsigned *status, cudaStream_t st);
+void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
+                  const float *SFf, float *FFf, float *UFf, double *GF, unsigned *status,
+                  cudaStream_t st);
+// cell pressure relaxation with the Newton iteration in FP32 and the energy-consistent
+// pressure and internal energies in FP64
+void ffv_m5f_relax_cell(int64_t n, const M5Consts &k, const double *Sin, double *Sout,
+                        uint8_t *flag, unsigned *status, cudaStream_t st);
 void ffv_m5_cfl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
                 unsigned long long *d_out, cudaStream_t st);

@@ -1,0 +1,896 @@
+// Model-5 FP32-flux form: face reconstruction, wave speeds, star states and HLLC /
+// ghost-fluid HLLC fluxes in FP32; FP64 where cancellation needs it.
+//
+// The algorithm is the FP64 form's (ffv_m5_fp64.cu, itself the reference's m5_* code), with
+// these precision choices:
+//   * MUSCL slopes and limiter in FP32.  Face values are formed in FP64 as the cell value
+//     plus the FP32 slope correction, because the stiffened-gas pressure recovery below
+//     divides and cancels the volume fractions and internal energies.
+//   * Pressure relaxation of a face or cell state: each material's initial pressure
+//     p_k = (gamma_k - 1)(alpha rho e_k - e_el) / alpha_k - gamma_k p_inf_k (a difference
+//     of two ~1e9 numbers for a liquid with p_inf 6e8, divided by alpha_k that can be
+//     1e-8) and the final energy-consistent equilibrium pressure and internal energies
+//     are FP64; the Newton iteration on the equilibrium pressure in between is FP32 (it
+//     only has to locate the volume fractions, which are then used in FP64).
+//   * The face record handed to the flux kernel holds the face state in FP32 plus each
+//     material's pressure recovered in FP64 (rounded once to FP32) and the last
+//     material's volume fraction (1 - sum in FP64: in FP32 that difference would lose a
+//     1e-6 fraction next to 1).
+//   * Wave speeds, star region, physical flux, HLLC and its ghost-fluid variant: FP32.
+//     Face fluxes are stored as FP32 and summed into the FP64 cell residual by
+//     m5_cell_update; the RK state stays FP64.
+// Compiled with FMA contraction (no bit-exactness goal here: the error against the FP64
+// form is measured instead).
+#include <math.h>
+
+#include "ffv_device.cuh"
+#include "ffv_m5.cuh"
+#include "ffv_m5_frame.cuh"
+
+namespace {
+
+// face record: [neq conserved | nmat pressures | last volume fraction]
+template <int N>
+struct RecL {
+  static constexpr int NEQ = K5<N>::NEQ, P = NEQ, AL = NEQ + N, SIZE = NEQ + N + 1;
+};
+
+// ------------------------------------------------------------------ EOS in FP32
+__device__ __forceinline__ void gmat_f(const float A[9], float G[9], float &Gmag) {
+  G[0] = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
+  G[1] = A[0] * A[3] + A[1] * A[4] + A[2] * A[5];
+  G[2] = A[0] * A[6] + A[1] * A[7] + A[2] * A[8];
+  G[3] = G[1];
+  G[4] = A[3] * A[3] + A[4] * A[4] + A[5] * A[5];
+  G[5] = A[3] * A[6] + A[4] * A[7] + A[5] * A[8];
+  G[6] = G[2];
+  G[7] = G[5];
+  G[8] = A[6] * A[6] + A[7] * A[7] + A[8] * A[8];
+  Gmag = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
+         G[2] * (G[3] * G[7] - G[4] * G[6]);
+}
+
+// e_el = mu / (4 |G|^(1/6)) tr((G - |G|^(1/3) I)^2)   (state_equation.c:269-317)
+__device__ __forceinline__ float elastic_energy_f(const float G[9], float Gmag, float mu) {
+  if (!(fabsf(Gmag) != 0.0f) || !(mu != 0.0f)) return 0.0f;
+  float g13 = cbrtf(fabsf(Gmag));
+  if (isnan(g13)) g13 = 0.0f;
+  const float d0 = G[0] - g13, d4 = G[4] - g13, d8 = G[8] - g13;
+  // tr(M^2) of the symmetric M = G - g13 I
+  const float tr = d0 * d0 + d4 * d4 + d8 * d8 + 2.0f * (G[1] * G[1] + G[2] * G[2] + G[5] * G[5]);
+  return mu / (4.0f * sqrtf(g13)) * tr;
+}
+
+// material stress -alpha p I - mu/|G|^(1/6) (G^2 - tr(G^2)/3 I - |G|^(1/3)(G - tr G/3 I)),
+// accumulated into st (state_equation.c:143-204)
+__device__ __forceinline__ void eos_stress_f(float st[3][3], float avf, float pr, const float G[9],
+                                             float Gmag, float mu, float (*ast)[3]) {
+  float s[9];
+  if ((fabsf(Gmag) != 0.0f) && (mu != 0.0f)) {
+    float G2[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        G2[i * 3 + j] = G[i * 3 + 0] * G[0 * 3 + j] + G[i * 3 + 1] * G[1 * 3 + j] +
+                        G[i * 3 + 2] * G[2 * 3 + j];
+    const float J1 = G[0] + G[4] + G[8], J2 = G2[0] + G2[4] + G2[8];
+    const float p13 = cbrtf(fabsf(Gmag));
+    const float f = mu / sqrtf(p13);
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      const bool dg = (q == 0 || q == 4 || q == 8);
+      const float ss = dg ? G2[q] - J2 * (1.0f / 3.0f) - p13 * (G[q] - J1 * (1.0f / 3.0f))
+                          : G2[q] - p13 * G[q];
+      s[q] = dg ? -avf * pr - f * ss : -f * ss;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 9; q++) s[q] = (q == 0 || q == 4 || q == 8) ? -avf * pr : 0.0f;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    st[q / 3][q % 3] += s[q];
+    if (ast) ast[q / 3][q % 3] = s[q];
+  }
+}
+
+template <int N>
+struct SolF {
+  float r, u, v, w, e, ut, vt, wt, c2;
+  double phi0;
+  float ra[N], avf[N], are[N], p[N];
+  float A[9], st[3][3];
+  float vec[K5<N>::NC];
+};
+
+// primitive state of a face record (m5_facercnstr.c:3-191 with the pressures given)
+template <int N>
+__device__ void make_sol_f(const M5Consts &k, const float *U, double phi0, SolF<N> &s) {
+  using C = K5<N>;
+  using RL = RecL<N>;
+  s.r = 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    s.r += U[i];
+    s.ra[i] = U[i];
+    s.vec[i] = U[i];
+  }
+  const float ir = 1.0f / s.r;
+  s.u = U[C::i1 + 0] * ir;
+  s.v = U[C::i1 + 1] * ir;
+  s.w = U[C::i1 + 2] * ir;
+#pragma unroll
+  for (int d = 0; d < 3; d++) s.vec[C::i1 + d] = U[C::i1 + d];
+  s.e = U[C::i2] * ir;
+  s.vec[C::i2] = U[C::i2];
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) s.avf[i] = U[C::i3 + i];
+  s.avf[N - 1] = U[RL::AL];
+  s.phi0 = phi0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) s.are[i] = U[C::i4 + i];
+#pragma unroll
+  for (int q = 0; q < 9; q++) s.A[q] = U[C::i5 + q];
+  float G[9], Gmag;
+  gmat_f(s.A, G, Gmag);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) s.st[i][j] = 0.0f;
+  float c2 = 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const float press = U[RL::P + i];
+    s.p[i] = press;
+    c2 += (s.avf[i] * ir) * (float)k.gamma[i] * (press + (float)k.pinf[i]);
+    eos_stress_f(s.st, s.avf[i], press, G, Gmag, (float)k.mu[i], nullptr);
+  }
+  s.c2 = c2;
+}
+
+// phi[0] of a cell (m5_facevalues.c:83-99): the solid fraction(s) against AVF_LIM, FP64
+template <int N>
+__device__ __forceinline__ double cell_phi0(const M5Consts &k, const double *__restrict__ S,
+                                            int64_t n, int64_t c) {
+  using C = K5<N>;
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double ac[N > 2 ? 2 : 1];
+#pragma unroll
+  for (int i = 0; i < (N > 2 ? 2 : 1); ++i) {
+    double a = S[(int64_t)(C::i3 + i) * n + c];
+    if (a >= hi) a = hi;
+    else if (a <= lo) a = lo;
+    ac[i] = a;
+  }
+  if (N > 2 && k.nsolids == 2 && k.mu[0] != 0.0)
+    return ((ac[0] > ac[N > 2 ? 1 : 0]) ? ac[0] : ac[N > 2 ? 1 : 0]) - k.avf_lim;
+  return ac[0] - k.avf_lim;
+}
+
+template <int F, int N>
+__device__ __forceinline__ void ghost_f(const SolF<N> &L, int bc, SolF<N> &R) {
+  R = L;
+  if (bc == 4 || bc == 5) {
+    const float v3[3] = {L.u, L.v, L.w};
+    const float ul = loc<F, 0>(v3), vl = loc<F, 1>(v3), wl = loc<F, 2>(v3);
+    const float ur = -ul, vr = bc == 5 ? -vl : vl, wr = bc == 5 ? -wl : wl;
+    R.u = glob<F, 0>(ur, vr, wr);
+    R.v = glob<F, 1>(ur, vr, wr);
+    R.w = glob<F, 2>(ur, vr, wr);
+  }
+}
+
+template <int N>
+struct NCf {
+  float unc[3], avf[N], are[N], A[9];
+};
+
+// m5_star_region.c:3-158 in FP32
+template <int F, int N>
+__device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const SolF<N> &L,
+                                  const SolF<N> &R, bool leftside, float u_S, float SL, float SR,
+                                  float uL, float vL, float wL, float uR, float vR, float wR,
+                                  const float sL[3], const float sR[3], float *Us, NCf<N> &nc) {
+  using C = K5<N>;
+  float SK, uK, vK, wK, s11K, s12K, s13K;
+  if (leftside) {
+    SK = SL; uK = uL; vK = vL; wK = wL; s11K = sL[0]; s12K = sL[1]; s13K = sL[2];
+  } else {
+    SK = SR; uK = uR; vK = vR; wK = wR; s11K = sR[0]; s12K = sR[1]; s13K = sR[2];
+  }
+  const float q = (SK - uK) / (SK - u_S);
+  float ar_S[N], r_S = 0.0f;
+#pragma unroll
+  for (int v = 0; v < N; ++v) {
+    ar_S[v] = s.ra[v] * q;
+    r_S += ar_S[v];
+  }
+  const float mR = (uR - SR) * R.r, mL = (uL - SL) * L.r;
+  const float iden = 1.0f / (mR - mL);
+  const float s11_S = (mR * sL[0] - mL * sR[0] + mL * mR * (uR - uL)) * iden;
+  float s12_S = 0.0f, s13_S = 0.0f;
+  if ((L.phi0 > 0.0) && (R.phi0 > 0.0)) {
+    s12_S = (mR * sL[1] - mL * sR[1] + mL * mR * (vR - vL)) * iden;
+    s13_S = (mR * sL[2] - mL * sR[2] + mL * mR * (wR - wL)) * iden;
+  }
+  const float ik = 1.0f / ((uK - SK) * s.r);
+  const float v_S = vK + (s12_S - s12K) * ik;
+  const float w_S = wK + (s13_S - s13K) * ik;
+  const float vel[3] = {glob<F, 0>(u_S, v_S, w_S), glob<F, 1>(u_S, v_S, w_S),
+                        glob<F, 2>(u_S, v_S, w_S)};
+  const float re = s.r * s.e;
+  const float Em_S = (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S +
+                      s12_S * v_S + s13_S * w_S) / (r_S * (u_S + SK));
+  float Am[3][3], Al[3][3], AS[3][3], Ag[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) Am[i][j] = s.A[3 * i + j];
+  tens_to_local<F>(Am, Al);
+  const float ius = 1.0f / (u_S - SK);
+#pragma unroll
+  for (int j = 0; j < 3; j++) {
+    AS[0][j] = (Al[0][j] * (uK - SK) - Al[1][j] * (vK - v_S) + Al[2][j] * (wK - w_S)) * ius;
+    AS[1][j] = Al[1][j];
+    AS[2][j] = Al[2][j];
+  }
+  tens_to_global<F>(AS, Ag);
+  float G[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      G[3 * i + j] = Ag[i][0] * Ag[j][0] + Ag[i][1] * Ag[j][1] + Ag[i][2] * Ag[j][2];
+  const float Gmag = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
+                     G[2] * (G[3] * G[7] - G[4] * G[6]);
+#pragma unroll
+  for (int v = 0; v < N; ++v) {
+    const float rm = s.ra[v] / s.avf[v];
+    const float rm_S = rm * (uK - SK) * ius;
+    const float ga = (float)k.gamma[v], pi = (float)k.pinf[v];
+    // the reference takes p_k = -p_hydro here (m5_star_region.c:122)
+    const float p_S = (-s.p[v] + pi) * (((ga - 1.0f) * rm + (ga + 1.0f) * rm_S) /
+                                       ((ga - 1.0f) * rm_S + (ga + 1.0f) * rm)) - pi;
+    const float ael = elastic_energy_f(G, Gmag, (float)k.mu[v]);
+    const float eel = ael / (s.avf[v] * rm_S);
+    const float e_S = (p_S + ga * pi) / (rm_S * (ga + 1.0f)) + eel;
+    nc.are[v] = ar_S[v] * e_S;
+  }
+#pragma unroll
+  for (int v = 0; v < N; ++v) Us[C::i0 + v] = ar_S[v];
+#pragma unroll
+  for (int v = 0; v < 3; ++v) Us[C::i1 + v] = r_S * vel[v];
+  Us[C::i2] = r_S * Em_S;
+#pragma unroll
+  for (int d = 0; d < 3; d++) nc.unc[d] = vel[d];
+#pragma unroll
+  for (int v = 0; v < N - 1; ++v) nc.avf[v] = s.avf[v];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) nc.A[3 * i + j] = Ag[i][j];
+  unsigned st = 0;
+#pragma unroll
+  for (int iv = 0; iv < C::NC; ++iv)
+    if (isnan(Us[iv])) st |= FFV_ST_NAN;
+  return st;
+}
+
+// m5_flux.c / m5_flux_gfm.c normal component along face F, FP32
+template <int F, int N>
+__device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, NCf<N> &nc, float *Fn) {
+  using C = K5<N>;
+  constexpr int a = Fr<F, 0>::ax, sg = Fr<F, 0>::sg;
+  const float vu = gfm ? s.ut : s.u, vv = gfm ? s.vt : s.v, vw = gfm ? s.wt : s.w;
+  const float vel[3] = {vu, vv, vw};
+  const float va = vel[a];
+#pragma unroll
+  for (int v = 0; v < N; v++) Fn[C::i0 + v] = sgn<sg>(va * s.ra[v]);
+#pragma unroll
+  for (int b = 0; b < 3; b++)
+    Fn[C::i1 + b] = sgn<sg>(gfm ? va * vel[b] * s.r - s.st[b][a] : va * vel[b] * s.r + s.st[b][a]);
+  Fn[C::i2] = sgn<sg>(s.r * s.e * va - s.st[a][0] * vu - s.st[a][1] * vv - s.st[a][2] * vw);
+  if (flag == 0 || flag == 3) {
+#pragma unroll
+    for (int d = 0; d < 3; d++) nc.unc[d] = vel[d];
+#pragma unroll
+    for (int v = 0; v < N - 1; ++v) nc.avf[v] = s.avf[v];
+#pragma unroll
+    for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
+#pragma unroll
+    for (int q = 0; q < 9; q++) nc.A[q] = gfm ? s.A[q] : -s.A[q];
+  }
+  const float ua = nc.unc[a];
+#pragma unroll
+  for (int v = 0; v < N - 1; ++v) Fn[C::i3 + v] = sgn<sg>(ua * nc.avf[v]);
+#pragma unroll
+  for (int v = 0; v < N; ++v) Fn[C::i4 + v] = sgn<sg>(ua * nc.are[v]);
+#pragma unroll
+  for (int q = 0; q < 9; q++) Fn[C::i5 + q] = sgn<sg>(ua * nc.A[q]);
+}
+
+// m5_hllc.c:3-95 / m5_hllc_gfm.c:3-100 in FP32: ff += A (F.n + corr)
+template <int F, int N>
+__device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, bool gfm,
+                               float Area, float *ff, float unc[3]) {
+  using C = K5<N>;
+  const float vl3[3] = {L.u, L.v, L.w}, vr3[3] = {R.u, R.v, R.w};
+  const float uL = loc<F, 0>(vl3), vL = loc<F, 1>(vl3), wL = loc<F, 2>(vl3);
+  float uR = loc<F, 0>(vr3), vR = loc<F, 1>(vr3), wR = loc<F, 2>(vr3);
+  if (gfm) {
+    vR = vL;
+    wR = wL;
+    L.ut = L.u;
+    L.vt = L.v;
+    L.wt = L.w;
+    R.ut = glob<F, 0>(uR, vR, wR);
+    R.vt = glob<F, 1>(uR, vR, wR);
+    R.wt = glob<F, 2>(uR, vR, wR);
+    R.vec[C::i1 + 0] = R.ut * R.r;
+    R.vec[C::i1 + 1] = R.vt * R.r;
+    R.vec[C::i1 + 2] = R.wt * R.r;
+    R.vec[C::i2] = R.r * R.e;
+  }
+  const float ruL = L.r * uL, ruR = R.r * uR;
+  const float cL = sqrtf(L.c2), cR = sqrtf(R.c2);
+  const float SR = fmaxf(uL + cL, uR + cR);
+  const float SL = fminf(uL - cL, uR - cR);
+  float TL[3][3], TR[3][3];
+  tens_to_local<F>(L.st, TL);
+  tens_to_local<F>(R.st, TR);
+  const float sL[3] = {TL[0][0], TL[0][1], TL[0][2]}, sR[3] = {TR[0][0], TR[0][1], TR[0][2]};
+  float u_S = ((L.r * (uL * uL) - sL[0]) - (R.r * (uR * uR) - sR[0]) - (SL * ruL) + (SR * ruR)) /
+              (ruL - ruR - (SL * L.r) + (SR * R.r));
+  unsigned st = (isnan(u_S) || isnan(SR) || isnan(SL)) ? FFV_ST_NAN_SPEED : 0u;
+  if (!gfm && bc == 4) u_S = 0.0f;
+  NCf<N> nc;
+  float Fn[C::NEQ], Us[C::NC], corr[C::NC];
+#pragma unroll
+  for (int iv = 0; iv < C::NC; ++iv) corr[iv] = 0.0f;
+  const bool left_star = gfm ? (SL < 0.0f && 0.0f <= u_S) : (SL <= 0.0f && 0.0f <= u_S);
+  const bool right_star = gfm ? (u_S < 0.0f && 0.0f < SR) : (u_S <= 0.0f && 0.0f <= SR);
+  if (0.0f <= SL) {
+    flux_n_f<F>(L, 0, gfm, nc, Fn);
+  } else if (left_star) {
+    st |= star_region_f<F>(k, L, L, R, true, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
+    flux_n_f<F>(L, 1, gfm, nc, Fn);
+#pragma unroll
+    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SL * (Us[iv] - L.vec[iv]);
+  } else if (right_star) {
+    st |= star_region_f<F>(k, R, L, R, false, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
+    flux_n_f<F>(R, 2, gfm, nc, Fn);
+#pragma unroll
+    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SR * (Us[iv] - R.vec[iv]);
+  } else if (SR <= 0.0f) {
+    flux_n_f<F>(R, 3, gfm, nc, Fn);
+  } else {
+    st |= FFV_ST_NO_BRANCH;
+#pragma unroll
+    for (int iv = 0; iv < C::NEQ; ++iv) Fn[iv] = 0.0f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) nc.unc[d] = 0.0f;
+  }
+#pragma unroll
+  for (int iv = 0; iv < C::NEQ; ++iv) ff[iv] += Area * (Fn[iv] + (iv < C::NC ? corr[iv] : 0.0f));
+#pragma unroll
+  for (int d = 0; d < 3; d++) unc[d] = nc.unc[d];
+  return st;
+}
+
+// ------------------------------------------------------------ relaxation, mixed precision
+template <int N>
+__device__ __forceinline__ void vf_limit_relax_d(const M5Consts &k, double *avf, bool elseif) {
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double sum = 0.0;
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) {
+    if (elseif) {
+      if (avf[i] <= lo) avf[i] = lo;
+      else if (avf[i] >= hi) avf[i] = hi;
+    } else {
+      if (avf[i] <= lo) avf[i] = lo;
+      if (avf[i] >= hi) avf[i] = hi;
+    }
+    sum += avf[i];
+  }
+  if (sum >= hi) {
+    const double dif = sum - hi;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) avf[j] = avf[j] - (avf[j] / sum) * dif;
+    sum = hi;
+  }
+  avf[N - 1] = 1.0 - sum;
+}
+
+// m5_relaxationvec.c's PRELAX 1 / 3 on V (FP64 state vector) with the Newton iteration in
+// FP32.  avf_out (optional) receives all N volume fractions and p_out the equilibrium
+// pressure (each material's pressure after relaxation).
+template <int N>
+__device__ unsigned relax_mixed(const M5Consts &k, double *V, double *avf_out, double *p_out) {
+  using C = K5<N>;
+  double ar[N], are[N], avf[N], avf0[N];
+  float A[9], G[9], Gmag;
+  double rho = 0.0;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) {
+    ar[iv] = V[iv + C::i0];
+    are[iv] = V[iv + C::i4];
+    rho += ar[iv];
+  }
+  const double irho = 1.0 / rho;
+  const double u = V[C::i1 + 0] * irho, v = V[C::i1 + 1] * irho, w = V[C::i1 + 2] * irho;
+  const double rE = V[C::i2];
+#pragma unroll
+  for (int iv = 0; iv < N - 1; ++iv) avf[iv] = V[iv + C::i3];
+  vf_limit_relax_d<N>(k, avf, true);
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) avf0[iv] = avf[iv];
+#pragma unroll
+  for (int q = 0; q < 9; q++) A[q] = (float)V[q + C::i5];
+  gmat_f(A, G, Gmag);
+  double ael[N];
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, (float)k.mu[iv]);
+  const double eps_sml = 1.0e-12, eps_big = 1.0e-8;
+  unsigned st = 0;
+  double ratio = 1.0;
+  if (k.prelax == 1) {  // closed form for two materials, FP64 (no iteration)
+    double t0[N], p0[N];
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) {
+      t0[iv] = avf[iv] / ar[iv];
+      p0[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) - k.gamma[iv] * k.pinf[iv];
+    }
+    const double *ga = k.gamma, *pi = k.pinf;
+    const double w0 = avf[0] / ga[0], w1 = avf[1] / ga[1];
+    const double A_1 = w0 * (p0[0] + pi[0]) / (w0 + w1);
+    const double A_2 = w1 * (p0[1] + pi[1]) / (w0 + w1);
+    const double d = (A_2 - A_1 - (pi[1] - pi[0]));
+    const double pe = 0.5 * (A_1 + A_2 - (pi[0] + pi[1])) + sqrt(0.25 * (d * d) + A_1 * A_2);
+    if (isnan(pe)) st |= FFV_ST_NAN;
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) {
+      const double t1 = t0[iv] * (p0[iv] + ga[iv] * pi[iv] + (ga[iv] - 1.0) * pe) /
+                        (pe + ga[iv] * pi[iv] + (ga[iv] - 1.0) * pe);
+      avf[iv] = ar[iv] * t1;
+    }
+    vf_limit_relax_d<N>(k, avf, false);
+    ratio = avf[0] / avf0[0];
+  } else {  // PRELAX 3
+    double pkinit[N];
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) {
+      if (avf[iv] < 0.0 || ar[iv] < 0.0) {
+        avf[iv] = eps_sml;
+        ar[iv] = eps_sml;
+        are[iv] = eps_sml;
+      }
+      if (avf[iv] >= 1.0) avf[iv] = 1.0 - eps_sml;
+    }
+    bool irelax = true;
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv)
+      if (avf[iv] > 1.0 - eps_sml) irelax = false;
+    if (irelax) {
+      double p0 = 0.0;
+#pragma unroll
+      for (int iv = 0; iv < N; ++iv) {
+        if (avf[iv] > eps_sml) {
+          // stiffened-gas pressure recovery: FP64
+          pkinit[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) -
+                       k.gamma[iv] * k.pinf[iv];
+          const double floor_p = -(1.0 - eps_big) * k.pinf[iv] + eps_big;
+          if (pkinit[iv] <= floor_p) pkinit[iv] = floor_p;
+        } else {
+          pkinit[iv] = 0.0;
+        }
+        p0 += avf[iv] * pkinit[iv];
+      }
+      // Newton on sum_k alpha_k(p) = 1 along each material's isentrope,
+      // alpha_k(p) = alpha_k0 ((p + pi_k) / (pk_k + pi_k))^(-1/gamma_k), in FP32.  The sum is
+      // formed in delta form, F = (sum_k alpha_k0 - 1) + sum_k alpha_k0 e_k with
+      // e_k = expm1(-log1p(x_k) / gamma_k), x_k = (p - pk_k) / (pk_k + pi_k), so that every
+      // term keeps FP32 precision relative to its own size: summing alpha_k(p) - 1 directly
+      // would resolve a 1e-6 volume fraction next to 1 - 1e-6 only to ~6e-8, which
+      // p_inf = 6e8 turns into ~200 Pa.
+      float a0[N], pkf[N], pif[N], b0[N], ig[N], e[N], plo[N], preset[N];
+      double sum0 = -1.0;
+#pragma unroll
+      for (int iv = 0; iv < N; ++iv) {
+        if (avf[iv] > eps_sml) sum0 += avf[iv];
+        a0[iv] = (float)avf[iv];
+        pkf[iv] = (float)pkinit[iv];
+        pif[iv] = (float)k.pinf[iv];
+        b0[iv] = (float)(1.0 / (pkinit[iv] + k.pinf[iv]));
+        ig[iv] = (float)(1.0 / k.gamma[iv]);
+        plo[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + eps_big);
+        preset[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + 1.0);
+        e[iv] = 0.0f;
+      }
+      const float F0 = (float)sum0;
+      float pf = (float)p0, F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
+      // the iterate settles within a few steps; the cap bounds the loop
+#pragma unroll 1
+      for (int iter = 0; iter < 64; iter++) {
+        const float step = F / dF;
+        if (iter > 0 && !(fabsf(step) > 1.0e-7f * fabsf(pf))) break;
+        pf = pf - step;
+#pragma unroll
+        for (int iv = 0; iv < N; ++iv)
+          if (pf < plo[iv]) pf = preset[iv];
+        if (pf == prev1 || pf == prev2) break;
+        F = F0;
+        dF = 0.0f;
+#pragma unroll
+        for (int iv = 0; iv < N; ++iv) {
+          if (avf[iv] > eps_sml) {
+            const float x = (pf - pkf[iv]) * b0[iv];
+            // 1 + x = (p + pi) / (pk + pi); near the pressure floor it is formed directly
+            const float opx = x > -0.5f ? 1.0f + x : fmaxf((pf + pif[iv]) * b0[iv], 1.0e-30f);
+            const float lx = x > -0.5f ? log1pf(x) : logf(opx);
+            e[iv] = expm1f(-lx * ig[iv]);
+            F += a0[iv] * e[iv];
+            dF -= a0[iv] * (1.0f + e[iv]) * ig[iv] * b0[iv] / opx;
+          }
+        }
+        if (isnan(pf) || isnan(F) || isnan(dF)) {
+          st |= FFV_ST_NAN;
+          break;
+        }
+        prev2 = prev1;
+        prev1 = pf;
+      }
+#pragma unroll
+      for (int iv = 0; iv < N; ++iv)
+        if (avf[iv] > eps_sml) avf[iv] = avf[iv] + avf[iv] * (double)e[iv];
+      vf_limit_relax_d<N>(k, avf, true);
+    }
+    const int i_as = ((avf[0] < avf[1]) && (k.mu[1] != 0.0)) ? 1 : 0;
+    ratio = avf[i_as] / avf0[i_as];
+  }
+  // energy-consistent equilibrium pressure and internal energies: FP64
+  double e_elast = 0.0;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) e_elast += ael[iv] * irho;
+  const double e_hyd = rE * irho - 0.5 * (u * u + v * v + w * w) - e_elast;
+  double num = 0.0, den = 0.0;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) {
+    const double ig1 = 1.0 / (k.gamma[iv] - 1.0);
+    num += avf[iv] * (k.gamma[iv] * k.pinf[iv] * ig1);
+    den += avf[iv] * ig1;
+  }
+  const double p_relaxed = (rho * e_hyd - num) / den;
+#pragma unroll
+  for (int iv = 0; iv < N - 1; ++iv) {
+    if (isnan(avf[iv])) st |= FFV_ST_NAN;
+    V[iv + C::i3] = avf[iv];
+  }
+#pragma unroll
+  for (int iv = 0; iv < N; iv++) {
+    const double a2 = avf[iv] * (p_relaxed + k.gamma[iv] * k.pinf[iv]) / (k.gamma[iv] - 1.0) + ael[iv];
+    if (isnan(a2)) st |= FFV_ST_NAN;
+    V[iv + C::i4] = a2;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) V[q + C::i5] = V[q + C::i5] * ratio;
+  if (avf_out)
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) avf_out[iv] = avf[iv];
+  if (p_out) *p_out = p_relaxed;
+  return st;
+}
+
+// avf_limit.c:3-21 on a state vector
+template <int N>
+__device__ __forceinline__ void avf_limit_d(const M5Consts &k, double *S) {
+  using C = K5<N>;
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double sum = 0.0;
+#pragma unroll
+  for (int v = 0; v < N - 1; ++v) {
+    double a = S[C::i3 + v];
+    if (a <= lo) a = lo;
+    else if (a >= hi) a = hi;
+    S[C::i3 + v] = a;
+    sum += a;
+  }
+  if (sum > hi) {
+    const double dif = sum - hi;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) {
+      const double a = S[C::i3 + j];
+      S[C::i3 + j] = a - (a / sum) * dif;
+    }
+  }
+}
+
+// face record of a state V (FP64): conserved variables, the volume fractions as the FP64
+// form's make_sol clamps them, and each material's pressure recovered in FP64
+template <int N>
+__device__ void write_record(const M5Consts &k, const double *V, const double *press, float *out,
+                             int64_t stride) {
+  using C = K5<N>;
+  using RL = RecL<N>;
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double at[N], sum = 0.0;
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) {
+    at[i] = V[C::i3 + i];
+    if (at[i] <= lo) at[i] = lo;
+    else if (at[i] >= hi) at[i] = hi;
+    sum += at[i];
+  }
+  if (sum > hi) {
+    const double dif = sum - hi;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) at[j] = at[j] - (at[j] / sum) * dif;
+    sum = hi;
+  }
+  at[N - 1] = 1.0 - sum;
+#pragma unroll
+  for (int i = 0; i < C::NEQ; i++) out[i * stride] = (float)V[i];
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) out[(C::i3 + i) * stride] = (float)at[i];
+  out[RL::AL * stride] = (float)at[N - 1];
+  if (press) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) out[(RL::P + i) * stride] = (float)press[i];
+  } else {
+    float A[9], G[9], Gmag;
+#pragma unroll
+    for (int q = 0; q < 9; q++) A[q] = (float)V[C::i5 + q];
+    gmat_f(A, G, Gmag);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      const double ael = (double)elastic_energy_f(G, Gmag, (float)k.mu[i]);
+      const double p = ((k.gamma[i] - 1.0) * (V[C::i4 + i] - ael) / at[i]) - k.gamma[i] * k.pinf[i];
+      out[(RL::P + i) * stride] = (float)p;
+    }
+  }
+}
+
+template <int N>
+__device__ __forceinline__ void load_state(const double *__restrict__ S, int64_t n, int64_t c,
+                                           double *U) {
+#pragma unroll
+  for (int v = 0; v < K5<N>::NEQ; v++) U[v] = S[(int64_t)v * n + c];
+}
+
+// m5_facevalues_MUSCL.c:3-45 (iside 1): value across face f, volume fractions limited
+template <int N>
+__device__ void value_across_d(const M5Consts &k, const ffv_dmesh &m, const double *__restrict__ S,
+                               int64_t c, int f, uint32_t kind, const double *Sc, double *X) {
+  using C = K5<N>;
+  if (kind & FFV_FK_BC) {
+#pragma unroll
+    for (int i = 0; i < C::NEQ; i++) X[i] = Sc[i];
+  } else if (kind == FFV_FK_FINER) {
+    const int32_t *sg = m.sub + 4 * (int64_t)m.nbr[(int64_t)f * m.n + c];
+#pragma unroll
+    for (int i = 0; i < C::NEQ; i++) X[i] = 0.0;
+#pragma unroll 1
+    for (int q = 0; q < 4; q++) {
+      const int64_t o = sg[q];
+#pragma unroll
+      for (int i = 0; i < C::NEQ; i++) X[i] += S[(int64_t)i * m.n + o];
+    }
+#pragma unroll
+    for (int i = 0; i < C::NEQ; i++) X[i] *= 0.25;
+  } else {
+    load_state<N>(S, m.n, m.nbr[(int64_t)f * m.n + c], X);
+  }
+  avf_limit_d<N>(k, X);
+}
+
+// ------------------------------------------------------------------------------ kernels
+template <int N>
+__global__ void __launch_bounds__(128) m5f_recon_face(ffv_dmesh m, ffv_geom g, M5Consts k,
+                                                      const double *__restrict__ S,
+                                                      float *__restrict__ SF,
+                                                      unsigned *__restrict__ status) {
+  using C = K5<N>;
+  using RL = RecL<N>;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 6 * m.n) return;
+  const int f = (int)(t / m.n);
+  const int64_t c = t - (int64_t)f * m.n;
+  const int fo = fr_opp(f);
+  const uint32_t info = m.info[c];
+  const int l = ffv_info_level(info);
+  const uint32_t kf = ffv_face_kind(info, f), ko = ffv_face_kind(info, fo);
+  double SL[C::NEQ], X[C::NEQ];
+  load_state<N>(S, m.n, c, SL);
+  avf_limit_d<N>(k, SL);
+  float df[C::NEQ];
+  value_across_d<N>(k, m, S, c, f, kf, SL, X);
+#pragma unroll
+  for (int i = 0; i < C::NEQ; i++) df[i] = (float)(X[i] - SL[i]);
+  value_across_d<N>(k, m, S, c, fo, ko, SL, X);
+  const float idp = (float)(1.0 / g.dcc[l][face_class(kf)]);
+  const float idm = (float)(1.0 / g.dcc[l][face_class(ko)]);
+  const float cf = (float)g.dcf[l][face_class(kf)];
+  double out[C::NEQ];
+#pragma unroll
+  for (int i = 0; i < C::NEQ; i++) {
+    const float db = (float)(X[i] - SL[i]);
+    float grad = 0.0f;
+    if (!(kf & FFV_FK_BC) && fabsf(df[i]) > 1e-10f && !(i >= C::i4 && i < C::i5)) {
+      const float sf = df[i] * idp, sb = -db * idm;
+      if (sb * sf > 0.0f) grad = (fabsf(sb) > fabsf(sf)) ? sf : sb;
+    }
+    out[i] = SL[i] + (double)(cf * grad);
+  }
+  // m5_reconctruct.c:144-179: volume-fraction limits of the face state
+  const double lo = k.amin / 100.0;
+  double sum = 0.0;
+#pragma unroll
+  for (int iv = 0; iv < N - 1; ++iv) {
+    double a = out[iv + C::i3];
+    if (a <= lo) a = lo;
+    else if (a >= (1.0 - (2.0 * lo))) a = 1.0 - (2.0 * lo);
+    out[iv + C::i3] = a;
+    sum += a;
+  }
+  if (sum >= (1.0 - lo)) {
+    const double dif = sum - (1.0 - lo);
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) out[j + C::i3] -= (out[j + C::i3] / sum) * dif;
+  }
+  double p_eq;
+  const unsigned st = relax_mixed<N>(k, out, nullptr, &p_eq);
+  double press[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) press[i] = p_eq;
+  write_record<N>(k, out, press, SF + (int64_t)f * RL::SIZE * m.n + c, m.n);
+  if (st) atomicOr(status, st);
+}
+
+template <int N>
+__device__ __forceinline__ void load_record(const float *__restrict__ SF, int64_t n, int f,
+                                            int64_t c, float *U) {
+  using RL = RecL<N>;
+#pragma unroll
+  for (int v = 0; v < RL::SIZE; v++) U[v] = SF[((int64_t)f * RL::SIZE + v) * n + c];
+}
+
+// order 1: the record of a cell state
+template <int N>
+__device__ __forceinline__ void record_of_cell(const M5Consts &k, const double *__restrict__ S,
+                                               int64_t n, int64_t c, float *U) {
+  double V[K5<N>::NEQ];
+  load_state<N>(S, n, c, V);
+  write_record<N>(k, V, nullptr, U, 1);
+}
+
+template <int N, int F>
+__device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
+                            const double *__restrict__ S, const float *__restrict__ SF, int64_t c,
+                            uint32_t info, float *ff, float uf[3], double &gfm_face, unsigned &st,
+                            bool &owner) {
+  using C = K5<N>;
+  using RL = RecL<N>;
+  constexpr int FO = fr_opp(F);
+  const uint32_t kind = ffv_face_kind(info, F);
+  const int l = ffv_info_level(info);
+#pragma unroll
+  for (int iv = 0; iv < C::NEQ; iv++) ff[iv] = 0.0f;
+  uf[0] = uf[1] = uf[2] = 0.0f;
+  gfm_face = 0.0;
+  if (kind == FFV_FK_SAME && m.nbr[(int64_t)F * m.n + c] < c) {
+    owner = false;  // evaluated by the neighbour (flux reuse, m5_residual.c:80-99)
+    return;
+  }
+  float U[RL::SIZE];
+  SolF<N> L, R;
+  if (k.order == 2) load_record<N>(SF, m.n, F, c, U);
+  else record_of_cell<N>(k, S, m.n, c, U);
+  make_sol_f<N>(k, U, cell_phi0<N>(k, S, m.n, c), L);
+  if (kind & FFV_FK_BC) {
+    const int bc = (int)(kind & 7u);
+    ghost_f<F, N>(L, bc, R);
+    const bool gfm = L.phi0 * R.phi0 < 0.0;
+    if (gfm) gfm_face = 1.0;
+    st |= hllc_acc_f<F, N>(k, L, R, bc, gfm, (float)g.area[l], ff, uf);
+    return;
+  }
+  const int nsub = kind == FFV_FK_FINER ? 4 : 1;
+  const float A = (float)(kind == FFV_FK_FINER ? g.area[l + 1] : g.area[l]);
+  const int32_t *sg = kind == FFV_FK_FINER ? m.sub + 4 * (int64_t)m.nbr[(int64_t)F * m.n + c] : nullptr;
+#pragma unroll 1
+  for (int q = 0; q < nsub; q++) {
+    const int64_t o = sg ? sg[q] : m.nbr[(int64_t)F * m.n + c];
+    if (k.order == 2) load_record<N>(SF, m.n, FO, o, U);
+    else record_of_cell<N>(k, S, m.n, o, U);
+    make_sol_f<N>(k, U, cell_phi0<N>(k, S, m.n, o), R);
+    const bool gfm = L.phi0 * R.phi0 < 0.0;
+    if (gfm) gfm_face = 1.0;
+    float un[3];
+    st |= hllc_acc_f<F, N>(k, L, R, 0, gfm, A, ff, un);
+    const float inv = 1.0f / (float)nsub;
+    uf[0] = un[0] * inv;
+    uf[1] = un[1] * inv;
+    uf[2] = un[2] * inv;
+  }
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) m5f_face_flux(ffv_dmesh m, ffv_geom g, M5Consts k,
+                                                     const double *__restrict__ S,
+                                                     const float *__restrict__ SF,
+                                                     float *__restrict__ FF,
+                                                     float *__restrict__ UF,
+                                                     double *__restrict__ GF,
+                                                     unsigned *__restrict__ status) {
+  using C = K5<N>;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 6 * m.n) return;
+  const int f = (int)(t / m.n);
+  const int64_t c = t - (int64_t)f * m.n;
+  const uint32_t info = m.info[c];
+  float ff[C::NEQ], uf[3];
+  double gf = 0.0;
+  unsigned st = 0;
+  bool owner = true;
+  switch (f) {
+    case 0: face_flux_f<N, 0>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 1: face_flux_f<N, 1>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 2: face_flux_f<N, 2>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 3: face_flux_f<N, 3>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 4: face_flux_f<N, 4>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    default: face_flux_f<N, 5>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+  }
+  if (owner) {
+#pragma unroll
+    for (int iv = 0; iv < C::NEQ; iv++) FF[((int64_t)f * C::NEQ + iv) * m.n + c] = ff[iv];
+#pragma unroll
+    for (int d = 0; d < 3; d++) UF[((int64_t)f * 3 + d) * m.n + c] = uf[d];
+  }
+  GF[(int64_t)f * m.n + c] = gf;
+  if (st) atomicOr(status, st);
+}
+
+template <int N>
+__global__ void __launch_bounds__(128) m5f_relax_cell(int64_t n, M5Consts k,
+                                                      const double *__restrict__ Sin,
+                                                      double *__restrict__ Sout,
+                                                      uint8_t *__restrict__ flag,
+                                                      unsigned *__restrict__ status) {
+  using C = K5<N>;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double s[C::NEQ];
+  load_state<N>(Sin, n, c, s);
+  const double phi_old = s[C::i3] - k.avf_lim;
+  const unsigned st = relax_mixed<N>(k, s, nullptr, nullptr);
+  const double phi_new = (k.mu[0] != 0.0) ? s[C::i3] - k.avf_lim : phi_old;
+  flag[c] = (phi_old * phi_new < 0.0) ? 1 : 0;
+#pragma unroll
+  for (int e = 0; e < C::NEQ; e++) Sout[(int64_t)e * n + c] = s[e];
+  if (st) atomicOr(status, st);
+}
+
+}  // namespace
+
+void ffv_m5f_recon(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
+                   float *SFf, unsigned *status, cudaStream_t st) {
+  const unsigned blocks = (unsigned)((6 * m.n + 127) / 128);
+  if (k.nmat == 2) m5f_recon_face<2><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, status);
+  else m5f_recon_face<3><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, status);
+}
+
+void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
+                  const float *SFf, float *FFf, float *UFf, double *GF, unsigned *status,
+                  cudaStream_t st) {
+  const unsigned blocks = (unsigned)((6 * m.n + 127) / 128);
+  if (k.nmat == 2) m5f_face_flux<2><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, FFf, UFf, GF, status);
+  else m5f_face_flux<3><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, FFf, UFf, GF, status);
+}
+
+void ffv_m5f_relax_cell(int64_t n, const M5Consts &k, const double *Sin, double *Sout,
+                        uint8_t *flag, unsigned *status, cudaStream_t st) {
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+  if (k.nmat == 2) m5f_relax_cell<2><<<blocks, 128, 0, st>>>(n, k, Sin, Sout, flag, status);
+  else m5f_relax_cell<3><<<blocks, 128, 0, st>>>(n, k, Sin, Sout, flag, status);
+}

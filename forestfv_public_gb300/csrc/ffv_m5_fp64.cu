@@ -23,47 +23,9 @@
 
 #include "ffv_device.cuh"
 #include "ffv_m5.cuh"
+#include "ffv_m5_frame.cuh"
 
 namespace {
-
-template <int N>
-struct K5 {
-  static constexpr int NEQ = 3 * N + 12, NC = N + 4;
-  static constexpr int i0 = 0, i1 = N, i2 = N + 3, i3 = N + 4, i4 = 2 * N + 3, i5 = 3 * N + 3;
-};
-
-template <int S>
-__device__ __forceinline__ double sgn(double x) {
-  return S > 0 ? x : -x;
-}
-// frame of face F: local axis q (0 = n, 1 = t1, 2 = t2) -> global axis and sign
-template <int F, int Q> struct Fr {
-  static constexpr int ax = Q == 0 ? fr_n_axis(F) : (Q == 1 ? fr_t1_axis(F) : fr_t2_axis(F));
-  static constexpr int sg = Q == 0 ? fr_n_sign(F) : (Q == 1 ? fr_t1_sign(F) : fr_t2_sign(F));
-};
-template <int F, int Q>
-__device__ __forceinline__ double loc(const double v[3]) {
-  return sgn<Fr<F, Q>::sg>(v[Fr<F, Q>::ax]);
-}
-// global component A of a*n + b*t1 + c*t2
-template <int F, int A>
-__device__ __forceinline__ double glob(double a, double b, double c) {
-  return Fr<F, 0>::ax == A ? sgn<Fr<F, 0>::sg>(a)
-                           : (Fr<F, 1>::ax == A ? sgn<Fr<F, 1>::sg>(b) : sgn<Fr<F, 2>::sg>(c));
-}
-// R T R^T for the frame of F (rotate_vectors.c:73-106, rows n, t1, t2): a signed permutation
-template <int F>
-__device__ __forceinline__ void tens_to_local(const double T[3][3], double out[3][3]) {
-#define TL(I, J) out[I][J] = sgn<Fr<F, I>::sg * Fr<F, J>::sg>(T[Fr<F, I>::ax][Fr<F, J>::ax])
-  TL(0, 0); TL(0, 1); TL(0, 2); TL(1, 0); TL(1, 1); TL(1, 2); TL(2, 0); TL(2, 1); TL(2, 2);
-#undef TL
-}
-template <int F>
-__device__ __forceinline__ void tens_to_global(const double T[3][3], double out[3][3]) {
-#define TG(I, J) out[Fr<F, I>::ax][Fr<F, J>::ax] = sgn<Fr<F, I>::sg * Fr<F, J>::sg>(T[I][J])
-  TG(0, 0); TG(0, 1); TG(0, 2); TG(1, 0); TG(1, 1); TG(1, 2); TG(2, 0); TG(2, 1); TG(2, 2);
-#undef TG
-}
 
 // ------------------------------------------------------------------ EOS (state_equation.c)
 __device__ __forceinline__ void gmat_of(const double A[9], double G[9], double &Gmag) {
@@ -936,12 +898,12 @@ __device__ __forceinline__ void clamp_zerou(const M5Consts &k, double *s, const 
 
 // residual + RK stage (m5_RK.c): writes RHS and the new state into Snew; stage-1 cells
 // whose solid fraction crosses AVF_LIM get the partial update and a flag for m5_gfm_seq
-template <int N>
+template <int N, typename TF>
 __global__ void __launch_bounds__(128) m5_cell_update(ffv_dmesh m, ffv_geom g, M5Consts k,
                                                       const double *__restrict__ S,
                                                       double *__restrict__ SN,
-                                                      const double *__restrict__ FF,
-                                                      const double *__restrict__ UF,
+                                                      const TF *__restrict__ FF,
+                                                      const TF *__restrict__ UF,
                                                       double *__restrict__ RHS,
                                                       double *__restrict__ Snew,
                                                       uint8_t *__restrict__ flag,
@@ -973,12 +935,12 @@ __global__ void __launch_bounds__(128) m5_cell_update(ffv_dmesh m, ffv_geom g, M
       }                                                                                  \
     }                                                                                    \
     _Pragma("unroll") for (int iv = 0; iv < C::NEQ; iv++) {                              \
-      const double x = FF[((int64_t)ff * C::NEQ + iv) * m.n + fc];                       \
+      const double x = (double)FF[((int64_t)ff * C::NEQ + iv) * m.n + fc];               \
       rhs[iv] += sg < 0.0 ? -x : x;                                                      \
     }                                                                                    \
-    const double u0 = UF[((int64_t)ff * 3 + 0) * m.n + fc];                              \
-    const double u1 = UF[((int64_t)ff * 3 + 1) * m.n + fc];                              \
-    const double u2 = UF[((int64_t)ff * 3 + 2) * m.n + fc];                              \
+    const double u0 = (double)UF[((int64_t)ff * 3 + 0) * m.n + fc];                      \
+    const double u1 = (double)UF[((int64_t)ff * 3 + 1) * m.n + fc];                      \
+    const double u2 = (double)UF[((int64_t)ff * 3 + 2) * m.n + fc];                      \
     nonconservative<N, F>(g, Cs, ast, info, l, sg < 0.0 ? -u0 : u0, sg < 0.0 ? -u1 : u1, \
                           sg < 0.0 ? -u2 : u2, rhs);                                     \
   }
@@ -1366,14 +1328,23 @@ static void stage_impl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
   const unsigned nb = (unsigned)((m.n + CB - 1) / CB);
   Rec rec{ev, 0, names, st};
   if (ev) cudaEventRecord(ev[0], st);
+  const bool f32 = k.precision == FFV_FP32_FLUX;
+  // the FP32 form keeps its face states and fluxes in the same buffers, as floats
+  float *SFf = (float *)b.SF, *FFf = (float *)b.FF, *UFf = (float *)b.UF;
   if (k.order == 2) {
-    m5_recon_face<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.status);
-    rec(k_names[0]);
+    if (f32) ffv_m5f_recon(m, g, k, b.S, SFf, b.status, st);
+    else m5_recon_face<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.status);
+    rec(f32 ? "m5f_recon_face" : k_names[0]);
   }
-  m5_face_flux<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.FF, b.UF, b.GF, b.status);
-  rec(k_names[1]);
-  m5_cell_update<N><<<gc, tpb, 0, st>>>(m, g, k, b.S, b.SN, b.FF, b.UF, b.RHS, b.Snew, b.flag,
-                                        b.dt, irk, b.status);
+  if (f32) ffv_m5f_flux(m, g, k, b.S, SFf, FFf, UFf, b.GF, b.status, st);
+  else m5_face_flux<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.FF, b.UF, b.GF, b.status);
+  rec(f32 ? "m5f_face_flux" : k_names[1]);
+  if (f32)
+    m5_cell_update<N, float><<<gc, tpb, 0, st>>>(m, g, k, b.S, b.SN, FFf, UFf, b.RHS, b.Snew,
+                                                 b.flag, b.dt, irk, b.status);
+  else
+    m5_cell_update<N, double><<<gc, tpb, 0, st>>>(m, g, k, b.S, b.SN, b.FF, b.UF, b.RHS, b.Snew,
+                                                  b.flag, b.dt, irk, b.status);
   rec(k_names[2]);
   if (irk == 1) {
     flag_count<<<nb, CB, 0, st>>>(m.n, b.flag, b.bcount);
@@ -1386,8 +1357,9 @@ static void stage_impl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
                                     b.dt, 0);
     rec(k_names[6]);
   }
-  m5_relax_cell<N><<<gc, tpb, 0, st>>>(m.n, k, b.Snew, b.S, b.flag, b.status);
-  rec(k_names[7]);
+  if (f32) ffv_m5f_relax_cell(m.n, k, b.Snew, b.S, b.flag, b.status, st);
+  else m5_relax_cell<N><<<gc, tpb, 0, st>>>(m.n, k, b.Snew, b.S, b.flag, b.status);
+  rec(f32 ? "m5f_relax_cell" : k_names[7]);
   flag_count<<<nb, CB, 0, st>>>(m.n, b.flag, b.bcount);
   rec(k_names[8]);
   flag_scan<<<1, CB, 0, st>>>((int)nb, b.bcount, b.count);
