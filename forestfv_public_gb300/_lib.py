@@ -47,11 +47,37 @@ class ForestDesc(ctypes.Structure):
 
 _lib = None
 
+class TagParams(ctypes.Structure):
+    """ffv_tag_params (include/ffv.h): the reference's refinement-criterion inputs."""
+    _fields_ = [("uniform", ctypes.c_int32), ("lvl_uniform", ctypes.c_int32),
+                ("grad_prs", ctypes.c_int32), ("lvl_prs", ctypes.c_int32),
+                ("thr_prs", ctypes.c_double),
+                ("grad_rho", ctypes.c_int32), ("lvl_rho", ctypes.c_int32),
+                ("thr_rho", ctypes.c_double),
+                ("grad_vel", ctypes.c_int32), ("lvl_vel", ctypes.c_int32),
+                ("thr_vel", ctypes.c_double),
+                ("inter0", ctypes.c_int32), ("lvl_inter0", ctypes.c_int32),
+                ("lrs_inter0", ctypes.c_int32),
+                ("inter1", ctypes.c_int32), ("lvl_inter1", ctypes.c_int32),
+                ("lrs_inter1", ctypes.c_int32)]
+
+    @classmethod
+    def from_tuple(cls, t) -> "TagParams":
+        """From (uniform, lvl, prs, lvl, thr, rho, lvl, thr, vel, lvl, thr, inter0, lvl,
+        lrs, inter1, lvl, lrs), the order of the reference's input file lines."""
+        names = [f[0] for f in cls._fields_]
+        p = cls()
+        for name, v in zip(names, t):
+            setattr(p, name, float(v) if name.startswith("thr") else int(v))
+        return p
+
+
 EXPORTS = (
     "ffv_mesh_build", "ffv_mesh_ncells", "ffv_mesh_free", "ffv_mesh_export", "ffv_create",
     "ffv_destroy", "ffv_set_mesh", "ffv_upload_state", "ffv_download_state", "ffv_stage",
     "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
     "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
+    "ffv_tags", "ffv_tags_smooth",
 )
 
 
@@ -87,6 +113,8 @@ def lib() -> ctypes.CDLL:
     L.ffv_stage_kernel_name.argtypes = [vp, i32]
     L.ffv_stage_kernel_name.restype = ctypes.c_char_p
     L.ffv_launches_per_step.argtypes = [vp, ctypes.POINTER(i32)]
+    L.ffv_tags.argtypes = [vp, vp, ctypes.POINTER(TagParams), vp, vp, vp]
+    L.ffv_tags_smooth.argtypes = [vp, i32, vp]
     L.ffv_error_string.argtypes = [ctypes.c_int]
     L.ffv_error_string.restype = ctypes.c_char_p
     _lib = L

@@ -27,6 +27,8 @@ struct ffv_ctx {
   uint8_t *d_flag;
   int32_t *d_list, *d_bcount, *d_count;
   M5Consts m5;
+  // refinement tags
+  int32_t *d_SI, *d_SItmp, *d_split;
   unsigned int *d_status;
   unsigned long long *d_red;
   // pinned host scalars
@@ -64,6 +66,10 @@ void free_mesh_buffers(ffv_ctx *c) {
   cudaFree(c->d_list);
   cudaFree(c->d_bcount);
   cudaFree(c->d_count);
+  cudaFree(c->d_SI);
+  cudaFree(c->d_SItmp);
+  cudaFree(c->d_split);
+  c->d_SI = c->d_SItmp = c->d_split = nullptr;
   c->d_info = nullptr;
   c->d_nbr = c->d_sub = nullptr;
   c->d_S = c->d_SN = c->d_SF = nullptr;
@@ -103,6 +109,12 @@ int launch_stage(ffv_ctx *c, int irk, cudaEvent_t *ev = nullptr) {
 }
 
 __global__ void set_scalar(double *dst, double v) { *dst = v; }
+
+__global__ void set_uniform_split(int32_t *split, int64_t n, int32_t level) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    split[i] = level;
+}
 
 int queue_dt(ffv_ctx *c, double dt) {
   set_scalar<<<1, 1, 0, c->stream>>>(c->d_dt, dt);
@@ -471,6 +483,58 @@ int ffv_stream(ffv_ctx *c, void **stream) {
   if (!c || !stream) return FFV_ERR_ARG;
   *stream = (void *)c->stream;
   return FFV_OK;
+}
+
+int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split,
+             int32_t *split_raw, int32_t *si) {
+  if (!c || !m || !p || !split) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  if (m->n != c->n) return FFV_ERR_ARG;
+  if (p->inter0 == 0 && p->inter1 == 1) return FFV_ERR_ARG;  // m5_input.c:52 exits there
+  if (p->grad_vel == 1 && p->grad_rho != 1) return FFV_ERR_UNSUPPORTED;
+  if (c->p.model != 5 && (p->grad_prs || p->grad_rho || p->grad_vel || p->inter0))
+    return FFV_ERR_UNSUPPORTED;
+  ffv_m5_tagc t;
+  t.uniform = p->uniform; t.lvl_uniform = p->lvl_uniform;
+  t.prs = p->grad_prs; t.lvl_prs = p->lvl_prs; t.thr_prs = p->thr_prs;
+  t.rho = p->grad_rho; t.lvl_rho = p->lvl_rho; t.thr_rho = p->thr_rho;
+  t.vel = p->grad_vel; t.lvl_vel = p->lvl_vel; t.thr_vel = p->thr_vel;
+  t.inter0 = p->inter0; t.lvl0 = p->lvl_inter0; t.lrs0 = p->lrs_inter0;
+  t.inter1 = p->inter1; t.lvl1 = p->lvl_inter1; t.lrs1 = p->lrs_inter0 + p->lrs_inter1;
+  t.si_max = 0;
+  if (p->inter0 == 1 && p->inter1 == 1) t.si_max = t.lrs0 + t.lrs1;
+  if (p->inter0 == 1 && p->inter1 == 0) t.si_max = t.lrs0;
+  // inputset.c:106, m5_input.c:53
+  int32_t level_max = p->lvl_uniform;
+  for (int32_t l : {p->lvl_prs, p->lvl_rho, p->lvl_vel, p->lvl_inter0, p->lvl_inter1})
+    level_max = level_max > l ? level_max : l;
+  CK(cudaSetDevice(c->device));
+  const int64_t n = c->n;
+  if (!c->d_split) {
+    if (cudaMalloc(&c->d_SI, sizeof(int32_t) * 2 * n) != cudaSuccess ||
+        cudaMalloc(&c->d_SItmp, sizeof(int32_t) * 2 * n) != cudaSuccess ||
+        cudaMalloc(&c->d_split, sizeof(int32_t) * n) != cudaSuccess) {
+      cudaFree(c->d_SI);
+      cudaFree(c->d_SItmp);
+      cudaFree(c->d_split);
+      c->d_SI = c->d_SItmp = c->d_split = nullptr;
+      return FFV_ERR_NOMEM;
+    }
+  }
+  if (c->p.model == 5) {
+    ffv_m5_tags(c->dm, c->m5, t, c->d_S, c->d_SI, c->d_SItmp, c->d_split, c->stream);
+  } else {
+    set_uniform_split<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
+        c->d_split, n, t.uniform == 1 ? (t.lvl_uniform > 1 ? t.lvl_uniform : 1) : 1);
+    CK(cudaMemsetAsync(c->d_SI, 0, sizeof(int32_t) * 2 * n, c->stream));
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(split, c->d_split, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+  if (si)
+    CK(cudaMemcpyAsync(si, c->d_SI, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (split_raw) memcpy(split_raw, split, sizeof(int32_t) * n);
+  return ffv_tags_smooth(m, level_max, split);
 }
 
 int ffv_launches_per_step(const ffv_ctx *c, int32_t *n) {

@@ -43,3 +43,15 @@ void ffv_m5f_relax_cell(int64_t n, const M5Consts &k, const double *Sin, double 
                         uint8_t *flag, unsigned *status, cudaStream_t st);
 void ffv_m5_cfl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
                 unsigned long long *d_out, cudaStream_t st);
+
+// refinement criteria (criterionsplt.c, interface_location.c) with the derived values the
+// reference forms from its input (m5_input.c:50-57): lrs1 = lrs0 + lrs1 as given,
+// si_max = ADAPT_INTER_MAX
+struct ffv_m5_tagc {
+  int uniform, lvl_uniform, prs, lvl_prs, rho, lvl_rho, vel, lvl_vel;
+  int inter0, lvl0, lrs0, inter1, lvl1, lrs1, si_max;
+  double thr_prs, thr_rho, thr_vel;
+};
+// SI [2][n] (interface layers), SItmp scratch of the same size, split [n]
+void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, const double *S,
+                 int32_t *SI, int32_t *SItmp, int32_t *split, cudaStream_t st);

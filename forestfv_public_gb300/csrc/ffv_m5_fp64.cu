@@ -1290,7 +1290,187 @@ __global__ void m5_cfl_kernel(ffv_dmesh m, ffv_geom g, M5Consts k, const double 
   }
 }
 
+// ------------------------------------------------------------------ refinement tags
+// phi[v] of a cell (m5_facevalues.c:83-99): the clamped volume fractions against AVF_LIM
+// (phi[0] the larger of two solids' fractions when there are two)
+template <int N>
+__device__ __forceinline__ void cell_phi(const M5Consts &k, const double *__restrict__ S,
+                                         int64_t n, int64_t c, double phi[2]) {
+  using C = K5<N>;
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double ac[2] = {0.0, 0.0};
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) {
+    double a = S[(int64_t)(C::i3 + i) * n + c];
+    if (a <= lo) a = lo;
+    else if (a >= hi) a = hi;
+    ac[i] = a;
+  }
+  phi[0] = ac[0] - k.avf_lim;
+  phi[1] = ac[1] - k.avf_lim;
+  if (N > 2 && k.nsolids == 2 && k.mu[0] != 0.0)
+    phi[0] = ((ac[0] > ac[1]) ? ac[0] : ac[1]) - k.avf_lim;
+}
+
+// neighbour q (< count) of cell c across face f; count 0 for boundary faces
+__device__ __forceinline__ int face_neighbours(const ffv_dmesh &m, int64_t c, uint32_t info, int f,
+                                               int64_t nb[4]) {
+  const uint32_t kind = ffv_face_kind(info, f);
+  if (kind & FFV_FK_BC) return 0;
+  const int32_t s = m.nbr[(int64_t)f * m.n + c];
+  if (kind == FFV_FK_FINER) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) nb[q] = m.sub[4 * (int64_t)s + q];
+    return 4;
+  }
+  nb[0] = s;
+  return 1;
+}
+
+// interface_location.c:17-46: SI = 1 where phi changes sign across a face (the face loop
+// stops after the first face that shows a change)
+template <int N>
+__global__ void __launch_bounds__(128) m5_si_first(ffv_dmesh m, M5Consts k,
+                                                   const double *__restrict__ S,
+                                                   int32_t *__restrict__ SI) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.n) return;
+  const uint32_t info = m.info[c];
+  double pl[2], pr[2];
+  cell_phi<N>(k, S, m.n, c, pl);
+  int si0 = 0, si1 = 0;
+  bool hit = false;
+  for (int f = 0; f < 6 && !hit; f++) {
+    int64_t nb[4];
+    const int cnt = face_neighbours(m, c, info, f, nb);
+    for (int q = 0; q < cnt; q++) {
+      cell_phi<N>(k, S, m.n, nb[q], pr);
+      for (int v = 0; v < N - 1; ++v)
+        if (pl[v] * pr[v] < 0.0) {
+          if (v == 0) si0 = 1;
+          else si1 = 1;
+          hit = true;
+        }
+    }
+  }
+  SI[c] = si0;
+  SI[m.n + c] = si1;
+}
+
+// interface_location.c:52-80: layer lvl next to layer lvl - 1.  The reference updates in
+// place in leaf order, but a cell only reads neighbours' lvl - 1 entries and only writes
+// lvl into entries that were 0, so reading the previous layer's copy gives the same result.
+__global__ void __launch_bounds__(128) m5_si_layer(ffv_dmesh m, int lvl,
+                                                   const int32_t *__restrict__ SIin,
+                                                   int32_t *__restrict__ SIout) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.n) return;
+  const uint32_t info = m.info[c];
+  int s[2] = {SIin[c], SIin[m.n + c]};
+  bool hit = false;
+  for (int f = 0; f < 6 && !hit; f++) {
+    int64_t nb[4];
+    const int cnt = face_neighbours(m, c, info, f, nb);
+    for (int q = 0; q < cnt; q++)
+      for (int v = 0; v < 2; ++v)
+        if (SIin[(int64_t)v * m.n + nb[q]] == lvl - 1 && s[v] == 0) {
+          s[v] = lvl;
+          hit = true;
+        }
+  }
+  SIout[c] = s[0];
+  SIout[m.n + c] = s[1];
+}
+
+// relative jump |x_nb - x| / max(|x_nb|, |x|) (criterionsplt.c:83-89), 0 below 1e-8
+__device__ __forceinline__ double rel_jump(double x_cur, double x_nb) {
+  const double eps = 1.0e-8;
+  if ((fabs(x_nb) > eps) || (fabs(x_cur) > eps)) {
+    const double a = fabs(x_nb), b = fabs(x_cur);
+    return fabs(x_nb - x_cur) / ((a > b) ? a : b);
+  }
+  return 0.0;
+}
+
+// criterionsplt.c:3-140 per cell: the uniform level, the gradient criterion over every
+// sub-neighbour and the interface layers
+template <int N>
+__global__ void __launch_bounds__(128) m5_tag_split(ffv_dmesh m, M5Consts k, ffv_m5_tagc t,
+                                                    const double *__restrict__ S,
+                                                    const int32_t *__restrict__ SI,
+                                                    int32_t *__restrict__ split) {
+  using C = K5<N>;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.n) return;
+  int level = 1;
+  if (t.uniform == 1) level = level > t.lvl_uniform ? level : t.lvl_uniform;
+  if (t.prs == 1 || t.rho == 1 || t.vel == 1) {
+    const uint32_t info = m.info[c];
+    double s[C::NEQ];
+    load_state<N>(S, m.n, c, s);
+    Sol<N> L;
+    make_sol<N>(k, s, s, false, L);
+    double pL = 0.0;
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) pL += L.avf[iv] * L.p[iv];
+    double gp = 0.0, gr = 0.0, gv = 0.0;
+    for (int f = 0; f < 6; f++) {
+      int64_t nb[4];
+      const int cnt = face_neighbours(m, c, info, f, nb);
+      for (int q = 0; q < cnt; q++) {
+        load_state<N>(S, m.n, nb[q], s);
+        Sol<N> R;
+        make_sol<N>(k, s, s, false, R);
+        if (t.prs == 1) {
+          double pR = 0.0;
+#pragma unroll
+          for (int iv = 0; iv < N; ++iv) pR += R.avf[iv] * R.p[iv];
+          const double g = rel_jump(pL, pR);
+          gp = (g > gp) ? g : gp;
+        }
+        double grho = 0.0;
+        if (t.rho == 1) {
+          grho = rel_jump(L.r, R.r);
+          gr = (grho > gr) ? grho : gr;
+        }
+        // the reference's velocity criterion takes the density jump (criterionsplt.c:120)
+        if (t.vel == 1) gv = (grho > gv) ? grho : gv;
+      }
+    }
+    int lt = 1;
+    if (t.prs == 1 && fabs(gp) >= t.thr_prs) lt = t.lvl_prs;
+    if (t.rho == 1 && fabs(gr) >= t.thr_rho) lt = t.lvl_rho;
+    if (t.vel == 1 && fabs(gv) >= t.thr_vel) lt = t.lvl_vel;
+    level = level > lt ? level : lt;
+  }
+  if (t.inter0 != 0) {
+    for (int v = 0; v < 2; ++v) {
+      const int si = SI[(int64_t)v * m.n + c];
+      if (si >= 1 && si < t.lrs0) level = level > t.lvl0 ? level : t.lvl0;
+      if (si >= t.lrs0 && si < t.lrs1) level = level > t.lvl1 ? level : t.lvl1;
+    }
+  }
+  split[c] = level;
+}
+
 }  // namespace
+
+void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, const double *S,
+                 int32_t *SI, int32_t *SItmp, int32_t *split, cudaStream_t st) {
+  const unsigned gc = (unsigned)((m.n + 127) / 128);
+  if (t.inter0 != 0) {
+    if (k.nmat == 2) m5_si_first<2><<<gc, 128, 0, st>>>(m, k, S, SI);
+    else m5_si_first<3><<<gc, 128, 0, st>>>(m, k, S, SI);
+    for (int lvl = 2; lvl < t.si_max; lvl++) {
+      cudaMemcpyAsync(SItmp, SI, sizeof(int32_t) * 2 * m.n, cudaMemcpyDeviceToDevice, st);
+      m5_si_layer<<<gc, 128, 0, st>>>(m, lvl, SItmp, SI);
+    }
+  } else {
+    cudaMemsetAsync(SI, 0, sizeof(int32_t) * 2 * m.n, st);
+  }
+  if (k.nmat == 2) m5_tag_split<2><<<gc, 128, 0, st>>>(m, k, t, S, SI, split);
+  else m5_tag_split<3><<<gc, 128, 0, st>>>(m, k, t, S, SI, split);
+}
 
 void ffv_m5_cfl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
                 unsigned long long *d_out, cudaStream_t st) {

@@ -74,6 +74,22 @@ class Solver:
     def step_async(self, dt: float, nsteps: int = 1) -> None:
         _lib.check(_lib.lib().ffv_step_async(self._h, dt, nsteps), "ffv_step_async")
 
+    def tags(self, params, with_raw: bool = False):
+        """Refinement tags of the current state (ffv_tags): the smoothed target level per
+        cell; with_raw also returns the level before smoothing and the interface layers
+        SI [2, n].  params: a TagParams or the reference's 17 criterion inputs."""
+        if not isinstance(params, _lib.TagParams):
+            params = _lib.TagParams.from_tuple(params)
+        n = self.mesh.n
+        split = np.empty(n, np.int32)
+        raw = np.empty(n, np.int32) if with_raw else None
+        si = np.empty((2, n), np.int32) if with_raw else None
+        _lib.check(_lib.lib().ffv_tags(self._h, self.mesh.handle, ctypes.byref(params),
+                                       split.ctypes.data,
+                                       raw.ctypes.data if with_raw else None,
+                                       si.ctypes.data if with_raw else None), "ffv_tags")
+        return (split, raw, si) if with_raw else split
+
     def cfl_dt(self, cfl: float) -> float:
         out = ctypes.c_double()
         _lib.check(_lib.lib().ffv_cfl_dt(self._h, cfl, ctypes.byref(out)), "ffv_cfl_dt")

@@ -155,6 +155,34 @@ const char *ffv_stage_kernel_name(const ffv_ctx *ctx, int32_t i);
 /* Number of kernel launches one time step issues (for launch accounting). */
 int ffv_launches_per_step(const ffv_ctx *ctx, int32_t *n);
 
+/* Refinement criteria, the reference's input globals for its tagging (strdata.h:78-106;
+ * inputset.c:78-104, m5_input.c:39-57): a leaf's target level is the largest of the
+ * uniform level, the gradient criterion's level and the interface layers' levels. */
+typedef struct ffv_tag_params {
+  int32_t uniform, lvl_uniform;            /* CRT_UNIFORM, CRT_LVL_UNIFORM                */
+  int32_t grad_prs, lvl_prs; double thr_prs; /* CRT_GRAD_PRS (relative pressure jump)     */
+  int32_t grad_rho, lvl_rho; double thr_rho; /* CRT_GRAD_RHO (relative density jump)      */
+  int32_t grad_vel, lvl_vel; double thr_vel; /* CRT_GRAD_VEL (the reference evaluates it on
+                                              the density jump, criterionsplt.c:120; it
+                                              needs grad_rho)                             */
+  int32_t inter0, lvl_inter0, lrs_inter0;  /* CRT_ADAPT_INTER_0: SI layers 1..lrs0-1       */
+  int32_t inter1, lvl_inter1, lrs_inter1;  /* CRT_ADAPT_INTER_1: SI layers lrs0..lrs0+lrs1-1,
+                                              as the input file gives lrs1 (m5_input.c:50) */
+} ffv_tag_params;
+
+/* Refinement tags of the current device state, the counterpart of interface_location +
+ * criterionsplt (interface_location.c:7-86, criterionsplt.c:3-140; on the device) followed
+ * by criterionsmth (criterionsmth.c:3-58; on the host, in leaf order).  `m` is the mesh
+ * set on the context.  split[n] receives the smoothed target level per leaf; split_raw[n]
+ * (nullable) the level before smoothing; si[2 n] (nullable) the interface layer numbers
+ * SI[0], SI[1] as [2][n].  Model 5; model 0 supports the uniform criterion only (the
+ * reference's gradient criterion has no model-0 branch, criterionsplt.c:64-70). */
+int ffv_tags(ffv_ctx *ctx, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split,
+             int32_t *split_raw, int32_t *si);
+/* criterionsmth alone, in place on split[n] (host): level_max is the reference's LEVEL,
+ * the largest level any criterion names. */
+int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *split);
+
 const char *ffv_error_string(int code);
 
 /* No-allocation model-0 step -- no counterpart in the reference.

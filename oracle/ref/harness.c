@@ -24,7 +24,10 @@
  *                       `<case>.ct` but inputset.c:31-125 defines 35; the wrapper points it
  *                       at `<case>.m0ct`, a file laid out the way m0_input expects.
  *   loop                dumps the leaf list (topology, geometry, state) before and after
- *                       the reference's time loop (loop.c:3-41) and times the loop.
+ *                       the reference's time loop (loop.c:3-41) and times the loop; with
+ *                       a `<case>.tag` file it then runs the reference's own refinement
+ *                       tagging on the final state (interface_location, criterionsplt,
+ *                       criterionsmth) and dumps the tags.
  *
  * The dump format is read by oracle/refcase.py (read_dump).
  */
@@ -140,6 +143,8 @@ void __wrap_criterionsplt(struct RUN *run) {
   }
 }
 
+void __real_criterionsplt(struct RUN *run);
+
 /* ------------------------------------------------------------------ dump */
 static void put_i32(FILE *f, int32_t v) { fwrite(&v, 4, 1, f); }
 static void put_f64(FILE *f, double v) { fwrite(&v, 8, 1, f); }
@@ -189,6 +194,64 @@ static void dump(struct RUN *run, const char *tag, double loop_seconds, int64_t 
   fclose(f);
 }
 
+/* <case>.tag: one line per tag pass, the refinement criteria in the input file's terms
+ *   uniform lvl  prs lvl thr  rho lvl thr  vel lvl thr  inter0 lvl lrs  inter1 lvl lrs
+ * They are set right before each pass (the mesh generation at start-up keeps the .ct
+ * values), with the derived globals formed as inputset.c:106 and m5_input.c:50-57 form
+ * them.  Every pass starts from the same final state (interface_location and
+ * criterionsplt recompute SI and split for every leaf).  Output <run>.tags.bin: "FFVT",
+ * npass, n, then per pass and leaf SI[0], SI[1], the split level criterionsplt gives and
+ * the split level after criterionsmth. */
+static void tag_pass(struct RUN *run) {
+  FILE *fp = open_case_file(run, ".tag");
+  if (!fp) return;
+  int32_t n = 0;
+  for (struct BRANCH *c = run->topo->locl; c; c = c->lnxt) n++;
+  int32_t *out = NULL, npass = 0;
+  int u, lu, pr, lp, rh, lr, ve, lv, i0, l0, r0, i1, l1, r1;
+  double tp, tr, tv;
+  while (fscanf(fp, "%d %d %d %d %lf %d %d %lf %d %d %lf %d %d %d %d %d %d", &u, &lu, &pr, &lp,
+                &tp, &rh, &lr, &tr, &ve, &lv, &tv, &i0, &l0, &r0, &i1, &l1, &r1) == 17) {
+    CRT_UNIFORM = u; CRT_LVL_UNIFORM = lu;
+    CRT_GEO_AREA = 0; CRT_LVL_GEO_AREA = 0;
+    CRT_GRAD_PRS = pr; CRT_LVL_GRAD_PRS = lp; CRT_GRAD_PRS_THR = tp;
+    CRT_GRAD_RHO = rh; CRT_LVL_GRAD_RHO = lr; CRT_GRAD_RHO_THR = tr;
+    CRT_GRAD_VEL = ve; CRT_LVL_GRAD_VEL = lv; CRT_GRAD_VEL_THR = tv;
+    CRT_ADAPT_INTER_0 = i0; CRT_LVL_ADAPT_INTER_0 = l0; CRT_LRS_ADAPT_INTER_0 = r0;
+    CRT_ADAPT_INTER_1 = i1; CRT_LVL_ADAPT_INTER_1 = l1; CRT_LRS_ADAPT_INTER_1 = r0 + r1;
+    ADAPT_INTER_MAX = 0;
+    if (i0 == 1 && i1 == 1) ADAPT_INTER_MAX = CRT_LRS_ADAPT_INTER_0 + CRT_LRS_ADAPT_INTER_1;
+    if (i0 == 1 && i1 == 0) ADAPT_INTER_MAX = CRT_LRS_ADAPT_INTER_0;
+    LEVEL = max(max(max(max(lu, 0), lp), lr), lv);
+    LEVEL = max(max(LEVEL, l0), l1);
+    for (struct BRANCH *c = run->topo->locl; c; c = c->lnxt) c->el->SI[0] = c->el->SI[1] = 0;
+    if (CRT_ADAPT_INTER_0 != 0) interface_location(run);
+    __real_criterionsplt(run);
+    out = realloc(out, sizeof(int32_t) * 4 * (size_t)n * (size_t)(npass + 1));
+    int32_t *o = out + (size_t)4 * n * npass, i = 0;
+    for (struct BRANCH *c = run->topo->locl; c; c = c->lnxt, i++) {
+      o[4 * i + 0] = c->el->SI[0];
+      o[4 * i + 1] = c->el->SI[1];
+      o[4 * i + 2] = c->split;
+    }
+    criterionsmth(run);
+    i = 0;
+    for (struct BRANCH *c = run->topo->locl; c; c = c->lnxt, i++) o[4 * i + 3] = c->split;
+    npass++;
+  }
+  fclose(fp);
+  char path[4096];
+  snprintf(path, sizeof path, "%s.tags.bin", run->con->runname);
+  FILE *f = fopen(path, "wb");
+  if (!f) { fprintf(stderr, "harness: cannot write %s\n", path); exit(3); }
+  fwrite("FFVT", 1, 4, f);
+  put_i32(f, npass);
+  put_i32(f, n);
+  if (npass) fwrite(out, sizeof(int32_t), (size_t)4 * n * npass, f);
+  fclose(f);
+  free(out);
+}
+
 void __real_loop(struct RUN *run);
 void __wrap_loop(struct RUN *run) {
   dump(run, "init", 0.0, 0);
@@ -196,6 +259,7 @@ void __wrap_loop(struct RUN *run) {
   __real_loop(run);
   double t1 = MPI_Wtime();
   dump(run, "final", t1 - t0, (int64_t)NSTEP + 1);
+  tag_pass(run);
 }
 
 /* m5_init_domain.c does not compile as published; this replacement assigns each leaf one

@@ -96,6 +96,10 @@ class Case:
     # model 5: dict with avf_lim, prelax, amin and per-material lists pinf, gamma, mu,
     # rho0, p0 (u0, v0, w0 optional, >= 0 as m5_input.c:113-135 checks them)
     m5: dict | None = None
+    # refinement criteria of tag passes on the final state (harness .tag file), one tuple
+    # per pass: (uniform, lvl, prs, lvl, thr, rho, lvl, thr, vel, lvl, thr, inter0, lvl,
+    # lrs, inter1, lvl, lrs) as the reference's input file gives them
+    tags: tuple | None = None
 
     @property
     def neq(self) -> int:
@@ -195,6 +199,11 @@ def write_case(c: Case, d: str, name: str = "case") -> str:
     if c.refine:
         with open(base + ".rf", "w") as f:
             f.write(c.refine + "\n")
+    if c.tags is not None:
+        with open(base + ".tag", "w") as f:
+            for t in c.tags:
+                f.write(" ".join(repr(float(v)) if isinstance(v, float) else str(int(v))
+                                 for v in t) + "\n")
     if c.m5 and c.m5.get("mix"):
         with open(base + ".mix", "w") as f:
             f.write(c.m5["mix"] + "\n")
@@ -224,6 +233,7 @@ class Dump:
     dist_cf: np.ndarray
     dist_cc: np.ndarray
     S: np.ndarray
+    tags: np.ndarray | None = None  # [npass, n, 4]: SI[0], SI[1], split, smoothed split
 
 
 _LEAF_HDR = struct.Struct("<2i16i3dd2i")
@@ -272,7 +282,15 @@ def run_case(c: Case, workdir: str | None = None, timeout: float = 600.0):
         if r.returncode != 0 or not os.path.exists(run + ".final.bin"):
             raise RuntimeError(f"reference run failed rc={r.returncode}\n{r.stdout[-3000:]}\n"
                                f"{r.stderr[-3000:]}")
-        return read_dump(run + ".init.bin"), read_dump(run + ".final.bin"), r.stdout
+        final = read_dump(run + ".final.bin")
+        if os.path.exists(run + ".tags.bin"):
+            with open(run + ".tags.bin", "rb") as f:
+                buf = f.read()
+            assert buf[:4] == b"FFVT"
+            npass, n = struct.unpack_from("<2i", buf, 4)
+            final.tags = np.frombuffer(buf, dtype="<i4", count=4 * n * npass,
+                                       offset=12).reshape(npass, n, 4).copy()
+        return read_dump(run + ".init.bin"), final, r.stdout
     finally:
         if own:
             import shutil

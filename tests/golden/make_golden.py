@@ -76,6 +76,18 @@ M5_CASES = {
 }
 
 
+# refinement tag passes run on the final state of every model-5 case (the reference's own
+# interface_location / criterionsplt / criterionsmth): (uniform, lvl, prs, lvl, thr, rho, lvl,
+# thr, vel, lvl, thr, inter0, lvl, lrs, inter1, lvl, lrs) as the reference's input file gives
+# them
+TAG_PASSES = (
+    (1, 2, 0, 0, 0.0, 1, 5, 0.05, 0, 0, 0.0, 0, 0, 0, 0, 0, 0),
+    (1, 3, 1, 5, 0.3, 1, 5, 0.5, 0, 0, 0.0, 1, 4, 2, 1, 3, 1),
+    (0, 0, 1, 5, 0.01, 1, 4, 0.2, 1, 5, 0.9, 1, 5, 1, 0, 0, 0),
+    (1, 1, 1, 4, 0.02, 0, 0, 0.0, 0, 0, 0.0, 1, 5, 3, 0, 0, 0),
+)
+
+
 def config1_case() -> rc.Case:
     """Plain-method Sod problem of the 32^3 uniform forest: 4^3 trees at level 4, ideal
     gas, transmissive, MUSCL-HLLC, RK_STEPS 2, 100 steps.  The reference has no CFL
@@ -99,6 +111,9 @@ def save(name: str, c: rc.Case, keep_geom: bool) -> None:
     if c.model == 5:
         for key in ("avf_lim", "prelax", "amin", "pinf", "gamma", "mu"):
             d["m5_" + key] = np.asarray(c.m5[key])
+    if final.tags is not None:
+        d["tag_params"] = np.asarray(c.tags, dtype=np.float64)
+        d["tags"] = final.tags.astype(np.int8)
     if keep_geom:
         d.update(bc=final.bc.astype(np.int8), nn=final.nneig.astype(np.int8),
                  neigfc=final.neigfc.astype(np.int8), nb=final.nb, area=final.area,
@@ -115,6 +130,7 @@ def main() -> None:
     for name, (c, g) in CASES.items():
         save(name, c, g)
     for name, c in M5_CASES.items():
+        c.tags = TAG_PASSES
         save(name, c, True)
     save("m0_config1_sod32", config1_case(), False)
 
