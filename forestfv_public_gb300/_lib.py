@@ -78,6 +78,9 @@ EXPORTS = (
     "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
     "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
     "ffv_tags", "ffv_tags_smooth",
+    "ffv_mlp_create", "ffv_mlp_destroy", "ffv_mlp_get_params", "ffv_mlp_set_params",
+    "ffv_mlp_set_norm", "ffv_mlp_fields", "ffv_mlp_features", "ffv_mlp_forward",
+    "ffv_mlp_predict", "ffv_mlp_grad", "ffv_mlp_train",
 )
 
 
@@ -115,6 +118,18 @@ def lib() -> ctypes.CDLL:
     L.ffv_launches_per_step.argtypes = [vp, ctypes.POINTER(i32)]
     L.ffv_tags.argtypes = [vp, vp, ctypes.POINTER(TagParams), vp, vp, vp]
     L.ffv_tags_smooth.argtypes = [vp, i32, vp]
+    u64, f32 = ctypes.c_uint64, ctypes.c_float
+    L.ffv_mlp_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, u64]
+    L.ffv_mlp_destroy.argtypes = [vp]
+    L.ffv_mlp_get_params.argtypes = [vp, vp]
+    L.ffv_mlp_set_params.argtypes = [vp, vp]
+    L.ffv_mlp_set_norm.argtypes = [vp, vp, vp]
+    L.ffv_mlp_fields.argtypes = [vp, vp]
+    L.ffv_mlp_features.argtypes = [vp, vp, vp]
+    L.ffv_mlp_forward.argtypes = [vp, vp, i64, vp]
+    L.ffv_mlp_predict.argtypes = [vp, vp, vp]
+    L.ffv_mlp_grad.argtypes = [vp, vp, vp, i64, vp, vp]
+    L.ffv_mlp_train.argtypes = [vp, vp, vp, i64, i32, i32, f32, f32, u64, vp]
     L.ffv_error_string.argtypes = [ctypes.c_int]
     L.ffv_error_string.restype = ctypes.c_char_p
     _lib = L

@@ -32,6 +32,7 @@ SOURCES = {
     "ffv_m5_fp64.cu": ["--fmad=false"],
     "ffv_m5_fp32.cu": [],
     "ffv_noalloc.cu": [],
+    "ffv_mlp.cu": [],
 }
 
 

@@ -205,6 +205,20 @@ void ffv_fill_geom(const ffv_mesh *m, ffv_geom *g) {
   }
 }
 
+// a read-only view of a context for the indicator (ffv_mlp.cu)
+int ffv_ctx_view(ffv_ctx *c, int *device, cudaStream_t *st, ffv_dmesh *dm, const double **S,
+                 const M5Consts **k, int *model) {
+  if (!c) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  *device = c->device;
+  *st = c->stream;
+  *dm = c->dm;
+  *S = c->d_S;
+  *k = &c->m5;
+  *model = c->p.model;
+  return FFV_OK;
+}
+
 extern "C" {
 
 const char *ffv_error_string(int code) {

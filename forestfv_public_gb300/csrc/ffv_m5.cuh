@@ -55,3 +55,7 @@ struct ffv_m5_tagc {
 // SI [2][n] (interface layers), SItmp scratch of the same size, split [n]
 void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, const double *S,
                  int32_t *SI, int32_t *SItmp, int32_t *split, cudaStream_t st);
+
+// fields of the learned refinement indicator, F [5][n] float (ffv_mlp.cu gathers them)
+void ffv_m5_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
+                             cudaStream_t st);

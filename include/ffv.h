@@ -183,6 +183,38 @@ int ffv_tags(ffv_ctx *ctx, const ffv_mesh *m, const ffv_tag_params *p, int32_t *
  * the largest level any criterion names. */
 int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *split);
 
+/* Learned refinement indicator (no counterpart in the reference): a 135-64-64-1
+ * perceptron with GELU hidden layers and a sigmoid output over the 27-cell stencil of five
+ * per-cell fields (log rho, log p, alpha_0, |u|, von Mises stress), BF16 operands and FP32
+ * accumulation on the tensor cores, trained on the GPU with AdamW.  Parameters are one
+ * FP32 vector: W1 [64][135], b1 [64], W2 [64][64], b2 [64], w3 [64], b3. */
+#define FFV_MLP_NPARAM 12929
+#define FFV_MLP_INPUT_STRIDE 144 /* BF16 values per feature row (135 + zero padding) */
+typedef struct ffv_mlp ffv_mlp;
+int ffv_mlp_create(ffv_mlp **mlp, int device, uint64_t seed);
+int ffv_mlp_destroy(ffv_mlp *mlp);
+int ffv_mlp_get_params(ffv_mlp *mlp, float *params);
+int ffv_mlp_set_params(ffv_mlp *mlp, const float *params); /* also resets AdamW state */
+/* per-field normalisation of the features (mean, standard deviation; 5 each) */
+int ffv_mlp_set_norm(ffv_mlp *mlp, const float *mean, const float *stdev);
+/* the five per-cell fields of the context's state into F_dev (device, FP32 [5][n]) */
+int ffv_mlp_fields(ffv_ctx *ctx, float *F_dev);
+/* feature rows of the context's state into X_dev (device, BF16 [n][144]) */
+int ffv_mlp_features(ffv_ctx *ctx, ffv_mlp *mlp, void *X_dev);
+/* probabilities of n feature rows (device pointers) */
+int ffv_mlp_forward(ffv_mlp *mlp, const void *X_dev, int64_t n, float *prob_dev);
+/* features + forward of the context's state, probabilities to the host (n) */
+int ffv_mlp_predict(ffv_ctx *ctx, ffv_mlp *mlp, float *prob_host);
+/* gradient (host, FFV_MLP_NPARAM) and loss of the mean binary cross-entropy over the first
+ * B rows of X_dev / labels y_dev (device, FP32 0 or 1) */
+int ffv_mlp_grad(ffv_mlp *mlp, const void *X_dev, const float *y_dev, int64_t B,
+                 float *grad_host, float *loss_host);
+/* steps AdamW steps (beta 0.9, 0.999, eps 1e-8, decoupled weight decay wd on the weights)
+ * on batches of `batch` rows drawn from the N rows of X_dev / y_dev with a seeded hash
+ * (seed != 0); loss_host (nullable) receives each step's mean loss */
+int ffv_mlp_train(ffv_mlp *mlp, const void *X_dev, const float *y_dev, int64_t N, int32_t batch,
+                  int32_t steps, float lr, float wd, uint64_t seed, float *loss_host);
+
 const char *ffv_error_string(int code);
 
 /* No-allocation model-0 step -- no counterpart in the reference.
