@@ -33,6 +33,7 @@ SOURCES = {
     "ffv_m5_fp32.cu": [],
     "ffv_noalloc.cu": [],
     "ffv_mlp.cu": [],
+    "ffv_m0_tags.cu": [],
 }
 
 

@@ -110,12 +110,6 @@ int launch_stage(ffv_ctx *c, int irk, cudaEvent_t *ev = nullptr) {
 
 __global__ void set_scalar(double *dst, double v) { *dst = v; }
 
-__global__ void set_uniform_split(int32_t *split, int64_t n, int32_t level) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
-    split[i] = level;
-}
-
 int queue_dt(ffv_ctx *c, double dt) {
   set_scalar<<<1, 1, 0, c->stream>>>(c->d_dt, dt);
   return cuda_rc(cudaGetLastError());
@@ -207,7 +201,7 @@ void ffv_fill_geom(const ffv_mesh *m, ffv_geom *g) {
 
 // a read-only view of a context for the indicator (ffv_mlp.cu)
 int ffv_ctx_view(ffv_ctx *c, int *device, cudaStream_t *st, ffv_dmesh *dm, const double **S,
-                 const M5Consts **k, int *model) {
+                 const M5Consts **k, int *model, double *gamma0, double *pinf0) {
   if (!c) return FFV_ERR_ARG;
   if (!c->have_state) return FFV_ERR_STATE;
   *device = c->device;
@@ -216,6 +210,8 @@ int ffv_ctx_view(ffv_ctx *c, int *device, cudaStream_t *st, ffv_dmesh *dm, const
   *S = c->d_S;
   *k = &c->m5;
   *model = c->p.model;
+  *gamma0 = c->p.gamma[0];
+  *pinf0 = c->p.pinf[0];
   return FFV_OK;
 }
 
@@ -506,8 +502,7 @@ int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *sp
   if (m->n != c->n) return FFV_ERR_ARG;
   if (p->inter0 == 0 && p->inter1 == 1) return FFV_ERR_ARG;  // m5_input.c:52 exits there
   if (p->grad_vel == 1 && p->grad_rho != 1) return FFV_ERR_UNSUPPORTED;
-  if (c->p.model != 5 && (p->grad_prs || p->grad_rho || p->grad_vel || p->inter0))
-    return FFV_ERR_UNSUPPORTED;
+  if (c->p.model != 5 && p->inter0) return FFV_ERR_UNSUPPORTED;  // no volume fractions
   ffv_m5_tagc t;
   t.uniform = p->uniform; t.lvl_uniform = p->lvl_uniform;
   t.prs = p->grad_prs; t.lvl_prs = p->lvl_prs; t.thr_prs = p->thr_prs;
@@ -538,8 +533,7 @@ int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *sp
   if (c->p.model == 5) {
     ffv_m5_tags(c->dm, c->m5, t, c->d_S, c->d_SI, c->d_SItmp, c->d_split, c->stream);
   } else {
-    set_uniform_split<<<(unsigned)((n + 255) / 256), 256, 0, c->stream>>>(
-        c->d_split, n, t.uniform == 1 ? (t.lvl_uniform > 1 ? t.lvl_uniform : 1) : 1);
+    ffv_m0_tags(c->dm, c->p.gamma[0], c->p.pinf[0], t, c->d_S, c->d_split, c->stream);
     CK(cudaMemsetAsync(c->d_SI, 0, sizeof(int32_t) * 2 * n, c->stream));
   }
   CK(cudaGetLastError());

@@ -59,3 +59,10 @@ void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, co
 // fields of the learned refinement indicator, F [5][n] float (ffv_mlp.cu gathers them)
 void ffv_m5_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
                              cudaStream_t st);
+
+// model 0 (ffv_m0_tags.cu): the relative-jump criterion on cell states and the indicator
+// fields (log rho, log p, 1, |u|, 0)
+void ffv_m0_tags(const ffv_dmesh &m, double gamma, double pinf, const ffv_m5_tagc &t,
+                 const double *S, int32_t *split, cudaStream_t st);
+void ffv_m0_indicator_fields(int64_t n, double gamma, double pinf, const double *S, float *F,
+                             cudaStream_t st);

@@ -562,7 +562,25 @@ void init_params(float *P, uint64_t seed) {
 
 // defined in ffv_api.cu
 int ffv_ctx_view(ffv_ctx *ctx, int *device, cudaStream_t *st, ffv_dmesh *dm, const double **S,
-                 const M5Consts **k, int *model);
+                 const M5Consts **k, int *model, double *gamma0, double *pinf0);
+
+namespace {
+struct CtxView {
+  int device, model;
+  cudaStream_t st;
+  ffv_dmesh dm;
+  const double *S;
+  const M5Consts *k;
+  double gamma0, pinf0;
+};
+int view(ffv_ctx *ctx, CtxView &v) {
+  return ffv_ctx_view(ctx, &v.device, &v.st, &v.dm, &v.S, &v.k, &v.model, &v.gamma0, &v.pinf0);
+}
+void launch_fields(const CtxView &v, float *F) {
+  if (v.model == 5) ffv_m5_indicator_fields(v.dm.n, *v.k, v.S, F, v.st);
+  else ffv_m0_indicator_fields(v.dm.n, v.gamma0, v.pinf0, v.S, F, v.st);
+}
+}  // namespace
 
 extern "C" {
 
@@ -666,40 +684,31 @@ int ffv_mlp_set_norm(ffv_mlp *m, const float *mean, const float *stdev) {
 }
 
 int ffv_mlp_fields(ffv_ctx *ctx, float *F_dev) {
-  int device, model;
-  cudaStream_t st;
-  ffv_dmesh dm;
-  const double *S;
-  const M5Consts *k;
-  int rc = ffv_ctx_view(ctx, &device, &st, &dm, &S, &k, &model);
+  CtxView v;
+  int rc = view(ctx, v);
   if (rc != FFV_OK) return rc;
   if (!F_dev) return FFV_ERR_ARG;
-  if (model != 5) return FFV_ERR_UNSUPPORTED;
-  MCK(cudaSetDevice(device));
-  ffv_m5_indicator_fields(dm.n, *k, S, F_dev, st);
+  MCK(cudaSetDevice(v.device));
+  launch_fields(v, F_dev);
   MCK(cudaGetLastError());
-  MCK(cudaStreamSynchronize(st));
+  MCK(cudaStreamSynchronize(v.st));
   return FFV_OK;
 }
 
 int ffv_mlp_features(ffv_ctx *ctx, ffv_mlp *m, void *X_dev) {
   if (!m || !X_dev) return FFV_ERR_ARG;
-  int device, model;
-  cudaStream_t st;
-  ffv_dmesh dm;
-  const double *S;
-  const M5Consts *k;
-  int rc = ffv_ctx_view(ctx, &device, &st, &dm, &S, &k, &model);
+  CtxView v;
+  int rc = view(ctx, v);
   if (rc != FFV_OK) return rc;
-  if (model != 5) return FFV_ERR_UNSUPPORTED;
-  if (device != m->device) return FFV_ERR_ARG;
-  MCK(cudaSetDevice(device));
-  rc = ensure_cap(m, dm.n);
+  if (v.device != m->device) return FFV_ERR_ARG;
+  MCK(cudaSetDevice(v.device));
+  rc = ensure_cap(m, v.dm.n);
   if (rc != FFV_OK) return rc;
-  ffv_m5_indicator_fields(dm.n, *k, S, m->d_F, st);
-  mlp_gather<<<(unsigned)((dm.n + 127) / 128), 128, 0, st>>>(dm, m->d_F, m->d_norm, (bf16 *)X_dev);
+  launch_fields(v, m->d_F);
+  mlp_gather<<<(unsigned)((v.dm.n + 127) / 128), 128, 0, v.st>>>(v.dm, m->d_F, m->d_norm,
+                                                                  (bf16 *)X_dev);
   MCK(cudaGetLastError());
-  MCK(cudaStreamSynchronize(st));
+  MCK(cudaStreamSynchronize(v.st));
   return FFV_OK;
 }
 
@@ -715,25 +724,20 @@ int ffv_mlp_forward(ffv_mlp *m, const void *X_dev, int64_t n, float *prob_dev) {
 
 int ffv_mlp_predict(ffv_ctx *ctx, ffv_mlp *m, float *prob_host) {
   if (!m || !prob_host) return FFV_ERR_ARG;
-  int device, model;
-  cudaStream_t st;
-  ffv_dmesh dm;
-  const double *S;
-  const M5Consts *k;
-  int rc = ffv_ctx_view(ctx, &device, &st, &dm, &S, &k, &model);
+  CtxView v;
+  int rc = view(ctx, v);
   if (rc != FFV_OK) return rc;
-  if (model != 5) return FFV_ERR_UNSUPPORTED;
-  if (device != m->device) return FFV_ERR_ARG;
-  MCK(cudaSetDevice(device));
-  rc = ensure_cap(m, dm.n);
+  if (v.device != m->device) return FFV_ERR_ARG;
+  MCK(cudaSetDevice(v.device));
+  rc = ensure_cap(m, v.dm.n);
   if (rc != FFV_OK) return rc;
-  ffv_m5_indicator_fields(dm.n, *k, S, m->d_F, st);
-  mlp_gather<<<(unsigned)((dm.n + 127) / 128), 128, 0, st>>>(dm, m->d_F, m->d_norm, m->d_X);
+  launch_fields(v, m->d_F);
+  mlp_gather<<<(unsigned)((v.dm.n + 127) / 128), 128, 0, v.st>>>(v.dm, m->d_F, m->d_norm, m->d_X);
   MCK(cudaGetLastError());
-  rc = forward(m, m->d_X, dm.n, m->d_prob, st);
+  rc = forward(m, m->d_X, v.dm.n, m->d_prob, v.st);
   if (rc != FFV_OK) return rc;
-  MCK(cudaMemcpyAsync(prob_host, m->d_prob, sizeof(float) * dm.n, cudaMemcpyDeviceToHost, st));
-  MCK(cudaStreamSynchronize(st));
+  MCK(cudaMemcpyAsync(prob_host, m->d_prob, sizeof(float) * v.dm.n, cudaMemcpyDeviceToHost, v.st));
+  MCK(cudaStreamSynchronize(v.st));
   return FFV_OK;
 }
 

@@ -134,3 +134,35 @@ def collect(solver, indicator: Indicator, tag_params, dt: float, snapshots: int,
     X = torch.cat(Xs)
     y = torch.cat(ys).to(X.device)
     return X, y, tags_now, tags_future
+
+
+def coverage(flag_now: np.ndarray, flag_future: np.ndarray) -> tuple[float, int]:
+    """Fraction of the cells flagged at the future step that are flagged now, and the number
+    of cells flagged now."""
+    fut = flag_future.astype(bool)
+    return float((flag_now & fut).sum() / max(fut.sum(), 1)), int(flag_now.sum())
+
+
+def gain_report(indicator: Indicator, solver, tag_params, dt: float, snapshots: int, every: int,
+                horizon: int, threshold: float = 0.5) -> dict:
+    """On a run the network was not trained on: how many of the cells that the plain
+    criterion will flag `horizon` steps later are already marked at step n, by the
+    criterion alone and by the criterion together with the network."""
+    level = solver.mesh.level
+    cov_c, cov_u, n_c, n_u = [], [], 0, 0
+    for _ in range(snapshots):
+        now = needs_refinement(solver.tags(tag_params), level)
+        pred = indicator.predict(solver) > threshold
+        solver.step(dt, horizon)
+        fut = needs_refinement(solver.tags(tag_params), level)
+        a, na = coverage(now, fut)
+        b, nb = coverage(now | pred, fut)
+        cov_c.append(a)
+        cov_u.append(b)
+        n_c += na
+        n_u += nb
+        if every > horizon:
+            solver.step(dt, every - horizon)
+    return {"coverage_criterion": float(np.mean(cov_c)),
+            "coverage_criterion_and_network": float(np.mean(cov_u)),
+            "cells_marked_criterion": n_c, "cells_marked_criterion_and_network": n_u}

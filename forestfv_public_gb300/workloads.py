@@ -109,3 +109,25 @@ def mixture_state(mat: dict, a_gas: np.ndarray) -> np.ndarray:
     S[N + 3] = E
     S[N + 4] = a0
     return S
+
+
+def blast_m0(mesh: Mesh, center, radius: float, p_in: float = 10.0, p_out: float = 0.1,
+             rho_in: float = 1.0, rho_out: float = 0.125, gamma: float = 1.4) -> np.ndarray:
+    """Model-0 spherical blast at rest: (rho_in, p_in) inside the sphere, (rho_out, p_out)
+    outside; SoA state [5, n]."""
+    x = mesh.centroids()
+    inside = np.linalg.norm(x - np.asarray(center), axis=1) < radius
+    rho = np.where(inside, rho_in, rho_out)
+    p = np.where(inside, p_in, p_out)
+    S = np.zeros((5, mesh.n))
+    S[0] = rho
+    S[4] = p / (gamma - 1.0)
+    return S
+
+
+def random_blast_m0(mesh: Mesh, seed: int) -> np.ndarray:
+    """A seeded blast: centre uniform in [0.3, 0.7]^3, radius in [0.08, 0.2], pressure
+    ratio in [20, 200]."""
+    rng = np.random.default_rng(seed)
+    return blast_m0(mesh, rng.uniform(0.3, 0.7, 3), rng.uniform(0.08, 0.2),
+                    p_in=0.1 * rng.uniform(20.0, 200.0))

@@ -175,8 +175,9 @@ typedef struct ffv_tag_params {
  * by criterionsmth (criterionsmth.c:3-58; on the host, in leaf order).  `m` is the mesh
  * set on the context.  split[n] receives the smoothed target level per leaf; split_raw[n]
  * (nullable) the level before smoothing; si[2 n] (nullable) the interface layer numbers
- * SI[0], SI[1] as [2][n].  Model 5; model 0 supports the uniform criterion only (the
- * reference's gradient criterion has no model-0 branch, criterionsplt.c:64-70). */
+ * SI[0], SI[1] as [2][n].  Model 5 as the reference; for model 0 (extension: the
+ * reference's gradient criterion has no model-0 branch, criterionsplt.c:64-70) the same
+ * relative jumps of the cell states, and no interface layers. */
 int ffv_tags(ffv_ctx *ctx, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split,
              int32_t *split_raw, int32_t *si);
 /* criterionsmth alone, in place on split[n] (host): level_max is the reference's LEVEL,
@@ -197,7 +198,8 @@ int ffv_mlp_get_params(ffv_mlp *mlp, float *params);
 int ffv_mlp_set_params(ffv_mlp *mlp, const float *params); /* also resets AdamW state */
 /* per-field normalisation of the features (mean, standard deviation; 5 each) */
 int ffv_mlp_set_norm(ffv_mlp *mlp, const float *mean, const float *stdev);
-/* the five per-cell fields of the context's state into F_dev (device, FP32 [5][n]) */
+/* the five per-cell fields of the context's state into F_dev (device, FP32 [5][n]); for
+ * model 0 the volume fraction is 1 and the stress 0 */
 int ffv_mlp_fields(ffv_ctx *ctx, float *F_dev);
 /* feature rows of the context's state into X_dev (device, BF16 [n][144]) */
 int ffv_mlp_features(ffv_ctx *ctx, ffv_mlp *mlp, void *X_dev);

@@ -32,7 +32,9 @@ def test_tags_match_reference(name, built_lib):
     s.close()
 
 
-def test_tags_model0_uniform_only(built_lib):
+def test_tags_model0(built_lib):
+    """Model 0: uniform level, the relative-jump criterion on cell states (an extension of
+    the reference, which has no model-0 branch), no interface layers."""
     m = Mesh((2, 2, 2), uniform_leaves((2, 2, 2), 3))
     s = Solver()
     s.set_mesh(m)
@@ -41,6 +43,15 @@ def test_tags_model0_uniform_only(built_lib):
     s.upload_state(S)
     split = s.tags((1, 4, 0, 0, 0.0, 0, 0, 0.0, 0, 0, 0.0, 0, 0, 0, 0, 0, 0))
     assert (split == 4).all()  # one level per smoothing pass at most
+    grad = (1, 3, 1, 5, 0.1, 1, 5, 0.1, 0, 0, 0.0, 0, 0, 0, 0, 0, 0)
+    assert (s.tags(grad) == 3).all()  # no jumps in a uniform state
+    x = m.centroids()
+    S[0] = np.where(x[:, 0] < 0.5, 1.0, 0.125)
+    s.upload_state(S)
+    split, raw, _ = s.tags(grad, with_raw=True)
+    jump = np.abs(x[:, 0] - 0.5) < 0.5 / (1 << 2)  # the two cell layers at the discontinuity
+    assert (raw[jump] == 5).all() and (raw[~jump] == 3).all()
+    assert split.max() == 4  # one level per pass above the mesh
     with pytest.raises(FFVError):
-        s.tags((1, 4, 0, 0, 0.0, 1, 5, 0.1, 0, 0, 0.0, 0, 0, 0, 0, 0, 0))
+        s.tags((1, 4, 0, 0, 0.0, 0, 0, 0.0, 0, 0, 0.0, 1, 5, 2, 0, 0, 0))
     s.close()
