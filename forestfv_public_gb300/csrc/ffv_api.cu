@@ -278,6 +278,13 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
     }
     k.amin = p->amin;
     k.avf_lim = p->avf_lim;
+    for (int i = 0; i < FFV_MAX_MATERIALS; i++) {
+      const double gm1 = p->gamma[i] - 1.0;
+      k.gpi[i] = p->gamma[i] * p->pinf[i];
+      k.ig1[i] = gm1 != 0.0 ? 1.0 / gm1 : 0.0;
+      k.gpg[i] = k.gpi[i] * k.ig1[i];
+      k.igam[i] = p->gamma[i] != 0.0 ? 1.0 / p->gamma[i] : 0.0;
+    }
   }
   int rc = FFV_OK;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||

@@ -11,6 +11,10 @@ struct M5Consts {
   int zerou[3];
   double gamma[FFV_MAX_MATERIALS], pinf[FFV_MAX_MATERIALS], mu[FFV_MAX_MATERIALS];
   double amin, avf_lim;
+  // per material, for the FP32-flux form: gamma p_inf, 1 / (gamma - 1),
+  // gamma p_inf / (gamma - 1), 1 / gamma
+  double gpi[FFV_MAX_MATERIALS], ig1[FFV_MAX_MATERIALS], gpg[FFV_MAX_MATERIALS],
+      igam[FFV_MAX_MATERIALS];
 };
 
 struct ffv_m5_bufs {
@@ -29,14 +33,22 @@ void ffv_m5_fp64_stage(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
 int ffv_m5_launches_per_stage(const M5Consts &k, int irk);
 
 // FP32-flux form (ffv_m5_fp32.cu): face states and face fluxes in FP32.
-//   SFf: [6][neq + nmat][n] float -- the reconstructed, relaxed face state (conserved
-//        variables) followed by each material's pressure, recovered in FP64
+//   Sf:  [neq][n] float copy of the state, made by ffv_m5f_shadow (scratch)
+//   SFf: [6][neq + nmat + 1][n] float -- the reconstructed, relaxed face state followed by
+//        each material's pressure, recovered in FP64, and the last volume fraction
 //   FFf: [6][neq][n] float face fluxes (area-weighted), UFf: [6][3][n] float face velocity
+void ffv_m5f_shadow(int64_t n, const M5Consts &k, const double *S, float *Sf, cudaStream_t st);
 void ffv_m5f_recon(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
-                   float *SFf, unsigned *status, cudaStream_t st);
+                   const float *Sf, float *SFf, unsigned *status, cudaStream_t st);
 void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
                   const float *SFf, float *FFf, float *UFf, double *GF, unsigned *status,
                   cudaStream_t st);
+// residual + RK stage of the FP32-flux form (the face fluxes of all but the deformation
+// summed in FP64)
+void ffv_m5f_cell_update(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
+                         double *SN, const float *FFf, const float *UFf, double *RHS,
+                         double *Snew, uint8_t *flag, const double *dt, int irk, unsigned *status,
+                         cudaStream_t st);
 // cell pressure relaxation with the Newton iteration in FP32 and the energy-consistent
 // pressure and internal energies in FP64
 void ffv_m5f_relax_cell(int64_t n, const M5Consts &k, const double *Sin, double *Sout,

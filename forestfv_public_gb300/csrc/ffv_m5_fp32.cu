@@ -658,40 +658,282 @@ __device__ __forceinline__ void load_state(const double *__restrict__ S, int64_t
   for (int v = 0; v < K5<N>::NEQ; v++) U[v] = S[(int64_t)v * n + c];
 }
 
-// m5_facevalues_MUSCL.c:3-45 (iside 1): value across face f, volume fractions limited
+// ------------------------------------------------------------ FP32 face reconstruction
+// A face state is held as an FP32 copy of every variable plus FP64 values of its
+// "critical" slots -- the volume fractions, the materials' internal energies and the total
+// energy, which enter the stiffened-gas pressure recovery: j < N-1 is alpha_j, then
+// (alpha rho e)_0..N-1, then E.
 template <int N>
-__device__ void value_across_d(const M5Consts &k, const ffv_dmesh &m, const double *__restrict__ S,
-                               int64_t c, int f, uint32_t kind, const double *Sc, double *X) {
+__device__ __forceinline__ constexpr int crit_slot(int j) {
+  return j < N - 1 ? K5<N>::i3 + j : (j < 2 * N - 1 ? K5<N>::i4 + (j - (N - 1)) : K5<N>::i2);
+}
+
+// avf_limit.c:3-21 on an FP32 state
+template <int N>
+__device__ __forceinline__ void avf_limit_f(const M5Consts &k, float *S) {
+  using C = K5<N>;
+  const float lo = (float)(k.amin / 100.0), hi = (float)(1.0 - (k.amin / 100.0));
+  float sum = 0.0f;
+#pragma unroll
+  for (int v = 0; v < N - 1; ++v) {
+    float a = S[C::i3 + v];
+    if (a <= lo) a = lo;
+    else if (a >= hi) a = hi;
+    S[C::i3 + v] = a;
+    sum += a;
+  }
+  if (sum > hi) {
+    const float dif = sum - hi;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) S[C::i3 + j] -= (S[C::i3 + j] / sum) * dif;
+  }
+}
+
+// m5_facevalues_MUSCL.c:3-45 (iside 1) on the FP32 copy of the state
+template <int N>
+__device__ void value_across_f(const M5Consts &k, const ffv_dmesh &m, const float *__restrict__ Sf,
+                               int64_t c, int f, uint32_t kind, const float *sc, float *X) {
   using C = K5<N>;
   if (kind & FFV_FK_BC) {
 #pragma unroll
-    for (int i = 0; i < C::NEQ; i++) X[i] = Sc[i];
+    for (int i = 0; i < C::NEQ; i++) X[i] = sc[i];
   } else if (kind == FFV_FK_FINER) {
     const int32_t *sg = m.sub + 4 * (int64_t)m.nbr[(int64_t)f * m.n + c];
 #pragma unroll
-    for (int i = 0; i < C::NEQ; i++) X[i] = 0.0;
+    for (int i = 0; i < C::NEQ; i++) X[i] = 0.0f;
 #pragma unroll 1
     for (int q = 0; q < 4; q++) {
       const int64_t o = sg[q];
 #pragma unroll
-      for (int i = 0; i < C::NEQ; i++) X[i] += S[(int64_t)i * m.n + o];
+      for (int i = 0; i < C::NEQ; i++) X[i] += Sf[(int64_t)i * m.n + o];
     }
 #pragma unroll
-    for (int i = 0; i < C::NEQ; i++) X[i] *= 0.25;
+    for (int i = 0; i < C::NEQ; i++) X[i] *= 0.25f;
   } else {
-    load_state<N>(S, m.n, m.nbr[(int64_t)f * m.n + c], X);
+    const int64_t o = m.nbr[(int64_t)f * m.n + c];
+#pragma unroll
+    for (int i = 0; i < C::NEQ; i++) X[i] = Sf[(int64_t)i * m.n + o];
   }
-  avf_limit_d<N>(k, X);
+  avf_limit_f<N>(k, X);
+}
+
+// the critical slots across face f (neighbour, mean of four finer, or the cell itself at
+// a boundary) in FP64, volume fractions limited as avf_limit does: their slopes are
+// differences of nearly equal numbers (a liquid fraction 1 - 1e-6, an energy of 1e9), which
+// the FP32 copy cannot resolve
+template <int N>
+__device__ void crit_across(const M5Consts &k, const ffv_dmesh &m, const double *__restrict__ S,
+                            int64_t c, int f, uint32_t kind, const double *own, double *X) {
+  constexpr int NCR = 2 * N;
+  if (kind & FFV_FK_BC) {
+#pragma unroll
+    for (int j = 0; j < NCR; j++) X[j] = own[j];
+    return;
+  }
+  if (kind == FFV_FK_FINER) {
+    const int32_t *sg = m.sub + 4 * (int64_t)m.nbr[(int64_t)f * m.n + c];
+#pragma unroll
+    for (int j = 0; j < NCR; j++) X[j] = 0.0;
+#pragma unroll 1
+    for (int q = 0; q < 4; q++) {
+      const int64_t o = sg[q];
+#pragma unroll
+      for (int j = 0; j < NCR; j++) X[j] += S[(int64_t)crit_slot<N>(j) * m.n + o];
+    }
+#pragma unroll
+    for (int j = 0; j < NCR; j++) X[j] *= 0.25;
+  } else {
+    const int64_t o = m.nbr[(int64_t)f * m.n + c];
+#pragma unroll
+    for (int j = 0; j < NCR; j++) X[j] = S[(int64_t)crit_slot<N>(j) * m.n + o];
+  }
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double sum = 0.0;
+#pragma unroll
+  for (int j = 0; j < N - 1; ++j) {
+    double a = X[j];
+    if (a <= lo) a = lo;
+    else if (a >= hi) a = hi;
+    X[j] = a;
+    sum += a;
+  }
+  if (sum > hi) {
+    const double dif = sum - hi;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) X[j] -= (X[j] / sum) * dif;
+  }
+}
+
+// m5_relaxationvec.c on a face state: FP32 partial densities, momentum and deformation in
+// v, FP64 critical slots in cr; the pressure recovery and the energy-consistent equilibrium
+// in FP64 with the materials' constants gamma p_inf / (gamma - 1), 1 / (gamma - 1) and
+// gamma p_inf formed once on the host; the Newton iteration as relax_mixed's
+template <int N>
+__device__ unsigned relax_face(const M5Consts &k, float *v, double *cr, double &p_out) {
+  using C = K5<N>;
+  double ar[N], are[N], avf[N], avf0[N], ael[N];
+  float rf = 0.0f;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) {
+    rf += v[C::i0 + iv];
+    ar[iv] = (double)v[C::i0 + iv];
+    are[iv] = cr[N - 1 + iv];
+  }
+  const double rE = cr[2 * N - 1];
+  const float mx = v[C::i1], my = v[C::i1 + 1], mz = v[C::i1 + 2];
+  const double ke = (double)(0.5f * (mx * mx + my * my + mz * mz) / rf);
+#pragma unroll
+  for (int iv = 0; iv < N - 1; ++iv) avf[iv] = cr[iv];
+  vf_limit_relax_d<N>(k, avf, true);
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) avf0[iv] = avf[iv];
+  float G[9], Gmag;
+  gmat_f(v + C::i5, G, Gmag);
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, (float)k.mu[iv]);
+  const double eps_sml = 1.0e-12, eps_big = 1.0e-8;
+  unsigned st = 0;
+  float ratio = 1.0f;
+  if (k.prelax == 1) {  // closed form for two materials
+    double t0[N], p0[N];
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) {
+      t0[iv] = avf[iv] / ar[iv];
+      p0[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) - k.gpi[iv];
+    }
+    const double *ga = k.gamma, *pi = k.pinf;
+    const double w0 = avf[0] / ga[0], w1 = avf[1] / ga[1];
+    const double A_1 = w0 * (p0[0] + pi[0]) / (w0 + w1);
+    const double A_2 = w1 * (p0[1] + pi[1]) / (w0 + w1);
+    const double d = (A_2 - A_1 - (pi[1] - pi[0]));
+    const double pe = 0.5 * (A_1 + A_2 - (pi[0] + pi[1])) + sqrt(0.25 * (d * d) + A_1 * A_2);
+    if (isnan(pe)) st |= FFV_ST_NAN;
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv)
+      avf[iv] = ar[iv] * t0[iv] * (p0[iv] + k.gpi[iv] + (ga[iv] - 1.0) * pe) /
+                (pe + k.gpi[iv] + (ga[iv] - 1.0) * pe);
+    vf_limit_relax_d<N>(k, avf, false);
+    ratio = (float)avf[0] / (float)avf0[0];
+  } else {  // PRELAX 3
+    double pkinit[N];
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) {
+      if (avf[iv] < 0.0 || ar[iv] < 0.0) {
+        avf[iv] = eps_sml;
+        ar[iv] = eps_sml;
+        are[iv] = eps_sml;
+      }
+      if (avf[iv] >= 1.0) avf[iv] = 1.0 - eps_sml;
+    }
+    bool irelax = true;
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv)
+      if (avf[iv] > 1.0 - eps_sml) irelax = false;
+    if (irelax) {
+      double p0 = 0.0, sum0 = -1.0;
+      float a0[N], pkf[N], pif[N], b0[N], ig[N], e[N], plo[N], preset[N];
+#pragma unroll
+      for (int iv = 0; iv < N; ++iv) {
+        if (avf[iv] > eps_sml) {
+          pkinit[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) - k.gpi[iv];
+          const double floor_p = -(1.0 - eps_big) * k.pinf[iv] + eps_big;
+          if (pkinit[iv] <= floor_p) pkinit[iv] = floor_p;
+          sum0 += avf[iv];
+        } else {
+          pkinit[iv] = 0.0;
+        }
+        p0 += avf[iv] * pkinit[iv];
+        a0[iv] = (float)avf[iv];
+        pkf[iv] = (float)pkinit[iv];
+        pif[iv] = (float)k.pinf[iv];
+        // in FP64: at a material's pressure floor pk + p_inf is a few Pa beside 6e8
+        b0[iv] = (float)(1.0 / (pkinit[iv] + k.pinf[iv]));
+        ig[iv] = (float)k.igam[iv];
+        plo[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + eps_big);
+        preset[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + 1.0);
+        e[iv] = 0.0f;
+      }
+      const float F0 = (float)sum0;
+      float pf = (float)p0, F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
+#pragma unroll 1
+      for (int iter = 0; iter < 64; iter++) {
+        const float step = F / dF;
+        if (iter > 0 && !(fabsf(step) > 1.0e-7f * fabsf(pf))) break;
+        pf = pf - step;
+#pragma unroll
+        for (int iv = 0; iv < N; ++iv)
+          if (pf < plo[iv]) pf = preset[iv];
+        if (pf == prev1 || pf == prev2) break;
+        F = F0;
+        dF = 0.0f;
+#pragma unroll
+        for (int iv = 0; iv < N; ++iv) {
+          if (avf[iv] > eps_sml) {
+            const float x = (pf - pkf[iv]) * b0[iv];
+            const float opx = x > -0.5f ? 1.0f + x : fmaxf((pf + pif[iv]) * b0[iv], 1.0e-30f);
+            const float lx = x > -0.5f ? log1pf(x) : logf(opx);
+            e[iv] = expm1f(-lx * ig[iv]);
+            F += a0[iv] * e[iv];
+            dF -= a0[iv] * (1.0f + e[iv]) * ig[iv] * b0[iv] / opx;
+          }
+        }
+        if (isnan(pf) || isnan(F) || isnan(dF)) {
+          st |= FFV_ST_NAN;
+          break;
+        }
+        prev2 = prev1;
+        prev1 = pf;
+      }
+#pragma unroll
+      for (int iv = 0; iv < N; ++iv)
+        if (avf[iv] > eps_sml) avf[iv] = avf[iv] + avf[iv] * (double)e[iv];
+      vf_limit_relax_d<N>(k, avf, true);
+    }
+    const int i_as = ((avf[0] < avf[1]) && (k.mu[1] != 0.0)) ? 1 : 0;
+    ratio = (float)avf[i_as] / (float)avf0[i_as];
+  }
+  double num = 0.0, den = 0.0, sael = 0.0;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) {
+    num += avf[iv] * k.gpg[iv];
+    den += avf[iv] * k.ig1[iv];
+    sael += ael[iv];
+  }
+  const double p = (rE - ke - sael - num) / den;
+#pragma unroll
+  for (int iv = 0; iv < N - 1; ++iv) {
+    if (isnan(avf[iv])) st |= FFV_ST_NAN;
+    cr[iv] = avf[iv];
+  }
+#pragma unroll
+  for (int iv = 0; iv < N; iv++) {
+    const double a2 = avf[iv] * (p + k.gpi[iv]) * k.ig1[iv] + ael[iv];
+    if (isnan(a2)) st |= FFV_ST_NAN;
+    cr[N - 1 + iv] = a2;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; ++q) v[C::i5 + q] *= ratio;
+  p_out = p;
+  return st;
 }
 
 // ------------------------------------------------------------------------------ kernels
+// FP32 copy of the state for the reconstruction (made once per cell per stage)
+__global__ void m5f_shadow(int64_t count, const double *__restrict__ S, float *__restrict__ Sf) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    Sf[i] = (float)S[i];
+}
+
 template <int N>
 __global__ void __launch_bounds__(128) m5f_recon_face(ffv_dmesh m, ffv_geom g, M5Consts k,
                                                       const double *__restrict__ S,
+                                                      const float *__restrict__ Sf,
                                                       float *__restrict__ SF,
                                                       unsigned *__restrict__ status) {
   using C = K5<N>;
   using RL = RecL<N>;
+  constexpr int NCR = 2 * N;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= 6 * m.n) return;
   const int f = (int)(t / m.n);
@@ -700,50 +942,117 @@ __global__ void __launch_bounds__(128) m5f_recon_face(ffv_dmesh m, ffv_geom g, M
   const uint32_t info = m.info[c];
   const int l = ffv_info_level(info);
   const uint32_t kf = ffv_face_kind(info, f), ko = ffv_face_kind(info, fo);
-  double SL[C::NEQ], X[C::NEQ];
-  load_state<N>(S, m.n, c, SL);
-  avf_limit_d<N>(k, SL);
-  float df[C::NEQ];
-  value_across_d<N>(k, m, S, c, f, kf, SL, X);
+  float sl[C::NEQ], x[C::NEQ], df[C::NEQ];
 #pragma unroll
-  for (int i = 0; i < C::NEQ; i++) df[i] = (float)(X[i] - SL[i]);
-  value_across_d<N>(k, m, S, c, fo, ko, SL, X);
+  for (int i = 0; i < C::NEQ; i++) sl[i] = Sf[(int64_t)i * m.n + c];
+  avf_limit_f<N>(k, sl);
+  // FP64 critical slots of the cell (volume fractions limited as avf_limit does)
+  double cr[NCR];
+#pragma unroll
+  for (int j = 0; j < NCR; j++) cr[j] = S[(int64_t)crit_slot<N>(j) * m.n + c];
+  {
+    const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+    double sum = 0.0;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) {
+      double a = cr[j];
+      if (a <= lo) a = lo;
+      else if (a >= hi) a = hi;
+      cr[j] = a;
+      sum += a;
+    }
+    if (sum > hi) {
+      const double dif = sum - hi;
+#pragma unroll
+      for (int j = 0; j < N - 1; ++j) cr[j] -= (cr[j] / sum) * dif;
+    }
+  }
+  value_across_f<N>(k, m, Sf, c, f, kf, sl, x);
+#pragma unroll
+  for (int i = 0; i < C::NEQ; i++) df[i] = x[i] - sl[i];
+  value_across_f<N>(k, m, Sf, c, fo, ko, sl, x);
+  // the critical slots' differences in FP64
+  float dfc[NCR], dbc[NCR];
+  {
+    double xc[NCR];
+    crit_across<N>(k, m, S, c, f, kf, cr, xc);
+#pragma unroll
+    for (int j = 0; j < NCR; j++) dfc[j] = (float)(xc[j] - cr[j]);
+    crit_across<N>(k, m, S, c, fo, ko, cr, xc);
+#pragma unroll
+    for (int j = 0; j < NCR; j++) dbc[j] = (float)(xc[j] - cr[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < NCR; j++) df[crit_slot<N>(j)] = dfc[j];
   const float idp = (float)(1.0 / g.dcc[l][face_class(kf)]);
   const float idm = (float)(1.0 / g.dcc[l][face_class(ko)]);
   const float cf = (float)g.dcf[l][face_class(kf)];
-  double out[C::NEQ];
+  float corr[C::NEQ];
 #pragma unroll
   for (int i = 0; i < C::NEQ; i++) {
-    const float db = (float)(X[i] - SL[i]);
+    float db = x[i] - sl[i];
+#pragma unroll
+    for (int j = 0; j < NCR; j++)
+      if (i == crit_slot<N>(j)) db = dbc[j];
     float grad = 0.0f;
     if (!(kf & FFV_FK_BC) && fabsf(df[i]) > 1e-10f && !(i >= C::i4 && i < C::i5)) {
       const float sf = df[i] * idp, sb = -db * idm;
       if (sb * sf > 0.0f) grad = (fabsf(sb) > fabsf(sf)) ? sf : sb;
     }
-    out[i] = SL[i] + (double)(cf * grad);
+    corr[i] = cf * grad;
+    sl[i] += corr[i];  // the face value of the FP32 copy
   }
+#pragma unroll
+  for (int j = 0; j < NCR; j++) cr[j] += (double)corr[crit_slot<N>(j)];
   // m5_reconctruct.c:144-179: volume-fraction limits of the face state
-  const double lo = k.amin / 100.0;
-  double sum = 0.0;
+  {
+    const double lo = k.amin / 100.0;
+    double sum = 0.0;
 #pragma unroll
-  for (int iv = 0; iv < N - 1; ++iv) {
-    double a = out[iv + C::i3];
-    if (a <= lo) a = lo;
-    else if (a >= (1.0 - (2.0 * lo))) a = 1.0 - (2.0 * lo);
-    out[iv + C::i3] = a;
-    sum += a;
-  }
-  if (sum >= (1.0 - lo)) {
-    const double dif = sum - (1.0 - lo);
+    for (int iv = 0; iv < N - 1; ++iv) {
+      double a = cr[iv];
+      if (a <= lo) a = lo;
+      else if (a >= (1.0 - (2.0 * lo))) a = 1.0 - (2.0 * lo);
+      cr[iv] = a;
+      sum += a;
+    }
+    if (sum >= (1.0 - lo)) {
+      const double dif = sum - (1.0 - lo);
 #pragma unroll
-    for (int j = 0; j < N - 1; ++j) out[j + C::i3] -= (out[j + C::i3] / sum) * dif;
+      for (int j = 0; j < N - 1; ++j) cr[j] -= (cr[j] / sum) * dif;
+    }
   }
   double p_eq;
-  const unsigned st = relax_mixed<N>(k, out, nullptr, &p_eq);
-  double press[N];
+  const unsigned st = relax_face<N>(k, sl, cr, p_eq);
+  // the face record: FP32 state with the critical slots rounded from FP64, the volume
+  // fractions as make_sol limits them, the equilibrium pressure for every material
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double at[N], sum = 0.0;
 #pragma unroll
-  for (int i = 0; i < N; ++i) press[i] = p_eq;
-  write_record<N>(k, out, press, SF + (int64_t)f * RL::SIZE * m.n + c, m.n);
+  for (int i = 0; i < N - 1; ++i) {
+    at[i] = cr[i];
+    if (at[i] <= lo) at[i] = lo;
+    else if (at[i] >= hi) at[i] = hi;
+    sum += at[i];
+  }
+  if (sum > hi) {
+    const double dif = sum - hi;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) at[j] -= (at[j] / sum) * dif;
+    sum = hi;
+  }
+  at[N - 1] = 1.0 - sum;
+  float *out = SF + (int64_t)f * RL::SIZE * m.n + c;
+#pragma unroll
+  for (int j = N - 1; j < NCR; j++) sl[crit_slot<N>(j)] = (float)cr[j];
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) sl[C::i3 + i] = (float)at[i];
+#pragma unroll
+  for (int i = 0; i < C::NEQ; i++) out[(int64_t)i * m.n] = sl[i];
+  out[(int64_t)RL::AL * m.n] = (float)at[N - 1];
+  const float pf = (float)p_eq;
+#pragma unroll
+  for (int i = 0; i < N; ++i) out[(int64_t)(RL::P + i) * m.n] = pf;
   if (st) atomicOr(status, st);
 }
 
@@ -851,6 +1160,196 @@ __global__ void __launch_bounds__(128) m5f_face_flux(ffv_dmesh m, ffv_geom g, M5
   if (st) atomicOr(status, st);
 }
 
+// ZEROU masks and positivity (m5_RK.c), as the FP64 form's clamp_zerou
+template <int N>
+__device__ __forceinline__ void clamp_zerou_d(const M5Consts &k, double *s, const double *sn) {
+  using C = K5<N>;
+#pragma unroll
+  for (int v = 0; v < N; v++)
+    if (s[C::i0 + v] < 0.0) s[C::i0 + v] = sn[C::i0 + v];
+  constexpr int e5 = C::i5;
+  if (k.zerou[0]) {
+    s[C::i1 + 0] = sn[C::i1 + 0];
+    s[e5 + 1] = sn[e5 + 1]; s[e5 + 2] = sn[e5 + 2]; s[e5 + 3] = sn[e5 + 3]; s[e5 + 6] = sn[e5 + 6];
+  }
+  if (k.zerou[1]) {
+    s[C::i1 + 1] = sn[C::i1 + 1];
+    s[e5 + 1] = sn[e5 + 1]; s[e5 + 3] = sn[e5 + 3]; s[e5 + 5] = sn[e5 + 5]; s[e5 + 7] = sn[e5 + 7];
+  }
+  if (k.zerou[2]) {
+    s[C::i1 + 2] = sn[C::i1 + 2];
+    s[e5 + 2] = sn[e5 + 2]; s[e5 + 5] = sn[e5 + 5]; s[e5 + 6] = sn[e5 + 6]; s[e5 + 7] = sn[e5 + 7];
+  }
+}
+
+// m5_cell_update of the FP32-flux form: the face fluxes of the partial densities, momentum,
+// energy, volume fractions and internal energies are summed in FP64 (the energy fluxes of
+// opposite faces cancel to ~1e-12 of their size), those of the deformation in FP32; the
+// non-conservative terms (m5_residual.c:175-215) are formed in FP32 from the cell's
+// volume fractions, deformation and material stresses (pressures recovered in FP64) and
+// added to the FP64 residual; the RK stage, positivity, ZEROU and the stage-1 ghost-fluid
+// trigger as in the FP64 form.
+template <int N>
+__global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, M5Consts k,
+                                                       const double *__restrict__ S,
+                                                       double *__restrict__ SN,
+                                                       const float *__restrict__ FF,
+                                                       const float *__restrict__ UF,
+                                                       double *__restrict__ RHS,
+                                                       double *__restrict__ Snew,
+                                                       uint8_t *__restrict__ flag,
+                                                       const double *__restrict__ dtp, int irk,
+                                                       unsigned *__restrict__ status) {
+  using C = K5<N>;
+  constexpr int NA = C::i5;  // residual entries summed in FP64: all but the deformation
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m.n) return;
+  const uint32_t info = m.info[c];
+  const int l = ffv_info_level(info);
+  double s[C::NEQ];
+  load_state<N>(S, m.n, c, s);
+  // the cell's volume fractions (make_sol, cell form) and material stresses
+  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
+  double at[N], sum = 0.0;
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) {
+    at[i] = s[C::i3 + i];
+    if (at[i] <= lo) at[i] = lo;
+    else if (at[i] >= hi) at[i] = hi;
+    sum += at[i];
+  }
+  if (sum > hi) {
+    const double dif = sum - hi;
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) at[j] -= (at[j] / sum) * dif;
+    sum = hi;
+  }
+  at[N - 1] = 1.0 - sum;
+  float A[9], G[9], Gmag, avf[N], ast[N][3][3], st_all[3][3];
+#pragma unroll
+  for (int q = 0; q < 9; q++) A[q] = (float)s[C::i5 + q];
+  gmat_f(A, G, Gmag);
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) st_all[i][j] = 0.0f;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const float ael = elastic_energy_f(G, Gmag, (float)k.mu[i]);
+    const double p = ((k.gamma[i] - 1.0) * (s[C::i4 + i] - (double)ael) / at[i]) - k.gpi[i];
+    avf[i] = (float)at[i];
+    eos_stress_f(st_all, avf[i], (float)p, G, Gmag, (float)k.mu[i], ast[i]);
+  }
+  double rhs[NA];
+  float rhsA[9], nc[N - 1 + N + 9];
+#pragma unroll
+  for (int iv = 0; iv < NA; iv++) rhs[iv] = 0.0;
+#pragma unroll
+  for (int q = 0; q < 9; q++) rhsA[q] = 0.0f;
+#pragma unroll
+  for (int q = 0; q < N - 1 + N + 9; q++) nc[q] = 0.0f;
+#pragma unroll
+  for (int F = 0; F < 6; F++) {
+    int64_t fc = c;
+    int ff = F;
+    float sg = 1.0f;
+    const uint32_t kind = ffv_face_kind(info, F);
+    if (kind == FFV_FK_SAME) {
+      const int64_t o = m.nbr[(int64_t)F * m.n + c];
+      if (o < c) {
+        fc = o;
+        ff = fr_opp(F);
+        sg = -1.0f;
+      }
+    }
+#pragma unroll
+    for (int iv = 0; iv < NA; iv++) rhs[iv] += (double)(sg * FF[((int64_t)ff * C::NEQ + iv) * m.n + fc]);
+#pragma unroll
+    for (int q = 0; q < 9; q++) rhsA[q] += sg * FF[((int64_t)ff * C::NEQ + C::i5 + q) * m.n + fc];
+    const float un = sg * UF[((int64_t)ff * 3 + 0) * m.n + fc];
+    const float vn = sg * UF[((int64_t)ff * 3 + 1) * m.n + fc];
+    const float wn = sg * UF[((int64_t)ff * 3 + 2) * m.n + fc];
+    const float Af = (float)(kind == FFV_FK_FINER ? 4.0 * g.area[l + 1] : g.area[l]);
+    const int ax = fr_n_axis(F);
+    const float nn[3] = {ax == 0 ? (float)fr_n_sign(F) : 0.0f, ax == 1 ? (float)fr_n_sign(F) : 0.0f,
+                         ax == 2 ? (float)fr_n_sign(F) : 0.0f};
+    const float nx = nn[0], ny = nn[1], nz = nn[2];
+#pragma unroll
+    for (int iv = 0; iv < N - 1; ++iv) nc[iv] += Af * (avf[iv] * un * nx + avf[iv] * vn * ny + avf[iv] * wn * nz);
+#pragma unroll
+    for (int iv = 0; iv < N; ++iv) {
+      const float(*t)[3] = ast[iv];
+      nc[N - 1 + iv] += Af * (t[0][0] * un * nx + t[0][1] * vn * nx + t[0][2] * wn * nx +
+                              t[1][0] * un * ny + t[1][1] * vn * ny + t[1][2] * wn * ny +
+                              t[2][0] * un * nz + t[2][1] * vn * nz + t[2][2] * wn * nz);
+    }
+    const float A1 = A[0], A2 = A[1], A3 = A[2], B1 = A[3], B2 = A[4], B3 = A[5], C1 = A[6], C2 = A[7],
+                C3 = A[8];
+    float *R5 = nc + (2 * N - 1);
+    R5[0] += Af * ((A1 * vn * ny + A1 * wn * nz) + B1 * vn * nx - C1 * wn * nx);
+    R5[1] += Af * ((A2 * vn * ny + A2 * wn * nz) + B2 * vn * nx - C2 * wn * nx);
+    R5[2] += Af * ((A3 * vn * ny + A3 * wn * nz) + B3 * vn * nx - C3 * wn * nx);
+    R5[3] += Af * ((B1 * un * nx + B1 * wn * nz) + A1 * un * ny - C1 * wn * ny);
+    R5[4] += Af * ((B2 * un * nx + B2 * wn * nz) + A2 * un * ny - C2 * wn * ny);
+    R5[5] += Af * ((B3 * un * nx + B3 * wn * nz) + A3 * un * ny - C3 * wn * ny);
+    R5[6] += Af * ((C1 * un * nx + C1 * vn * ny) + A1 * un * nz - B1 * vn * nz);
+    R5[7] += Af * ((C2 * un * nx + C2 * vn * ny) + A2 * un * nz - B2 * vn * nz);
+    R5[8] += Af * ((C3 * un * nx + C3 * vn * ny) + A3 * un * nz - B3 * vn * nz);
+  }
+  double r[C::NEQ];
+#pragma unroll
+  for (int iv = 0; iv < NA; iv++) r[iv] = rhs[iv];
+#pragma unroll
+  for (int iv = 0; iv < N - 1; iv++) r[C::i3 + iv] += (double)nc[iv];
+#pragma unroll
+  for (int iv = 0; iv < N; iv++) r[C::i4 + iv] += (double)nc[N - 1 + iv];
+#pragma unroll
+  for (int q = 0; q < 9; q++) r[C::i5 + q] = (double)(rhsA[q] + nc[2 * N - 1 + q]);
+  unsigned st = 0;
+#pragma unroll
+  for (int iv = 0; iv < C::NEQ; iv++) {
+    if (isnan(r[iv])) st |= FFV_ST_NAN;
+    RHS[(int64_t)iv * m.n + c] = r[iv];
+  }
+  const double dt = *dtp, V = g.vol[l], iV = g.inv_vol[l];
+  double sn[C::NEQ];
+  if (irk == 1) {
+#pragma unroll
+    for (int e = 0; e < C::NEQ; e++) {
+      sn[e] = s[e];
+      SN[(int64_t)e * m.n + c] = s[e];
+    }
+  } else {
+    load_state<N>(SN, m.n, c, sn);
+  }
+  bool gfm = false;
+  if (irk == 1) {
+#pragma unroll
+    for (int v = 0; v < N - 1; ++v) {
+      if (k.mu[v] != 0.0) {
+        const int e = C::i3 + v;
+        const double phi_old = s[e] - k.avf_lim;
+        const double as_new = sn[e] + dt * (iV * r[e]);
+        if (phi_old * (as_new - k.avf_lim) < 0.0) gfm = true;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < C::NEQ; e++)
+      if (!gfm || e >= C::i2) s[e] = sn[e] + dt * (iV * r[e]);
+  } else {
+    const double a = irk == 2 ? 3.0 / 4.0 : (irk == 3 ? 1.0 / 3.0 : 1.0 / 2.0);
+    const double b = 1.0 - a;
+#pragma unroll
+    for (int e = 0; e < C::NEQ; e++) s[e] = a * sn[e] + b * s[e] + b * dt * r[e] * iV;
+  }
+  if (!gfm) clamp_zerou_d<N>(k, s, sn);
+#pragma unroll
+  for (int e = 0; e < C::NEQ; e++) Snew[(int64_t)e * m.n + c] = s[e];
+  flag[c] = gfm ? 1 : 0;
+  if (st) atomicOr(status, st);
+  (void)V;
+}
+
 template <int N>
 __global__ void __launch_bounds__(128) m5f_relax_cell(int64_t n, M5Consts k,
                                                       const double *__restrict__ Sin,
@@ -873,11 +1372,15 @@ __global__ void __launch_bounds__(128) m5f_relax_cell(int64_t n, M5Consts k,
 
 }  // namespace
 
+void ffv_m5f_shadow(int64_t n, const M5Consts &k, const double *S, float *Sf, cudaStream_t st) {
+  m5f_shadow<<<152 * 8, 256, 0, st>>>((int64_t)ffv_m5_neq(k.nmat) * n, S, Sf);
+}
+
 void ffv_m5f_recon(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
-                   float *SFf, unsigned *status, cudaStream_t st) {
+                   const float *Sf, float *SFf, unsigned *status, cudaStream_t st) {
   const unsigned blocks = (unsigned)((6 * m.n + 127) / 128);
-  if (k.nmat == 2) m5f_recon_face<2><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, status);
-  else m5f_recon_face<3><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, status);
+  if (k.nmat == 2) m5f_recon_face<2><<<blocks, 128, 0, st>>>(m, g, k, S, Sf, SFf, status);
+  else m5f_recon_face<3><<<blocks, 128, 0, st>>>(m, g, k, S, Sf, SFf, status);
 }
 
 void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
@@ -886,6 +1389,17 @@ void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, cons
   const unsigned blocks = (unsigned)((6 * m.n + 127) / 128);
   if (k.nmat == 2) m5f_face_flux<2><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, FFf, UFf, GF, status);
   else m5f_face_flux<3><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, FFf, UFf, GF, status);
+}
+
+void ffv_m5f_cell_update(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
+                         double *SN, const float *FFf, const float *UFf, double *RHS,
+                         double *Snew, uint8_t *flag, const double *dt, int irk, unsigned *status,
+                         cudaStream_t st) {
+  const unsigned blocks = (unsigned)((m.n + 127) / 128);
+  if (k.nmat == 2)
+    m5f_cell_update<2><<<blocks, 128, 0, st>>>(m, g, k, S, SN, FFf, UFf, RHS, Snew, flag, dt, irk, status);
+  else
+    m5f_cell_update<3><<<blocks, 128, 0, st>>>(m, g, k, S, SN, FFf, UFf, RHS, Snew, flag, dt, irk, status);
 }
 
 void ffv_m5f_relax_cell(int64_t n, const M5Consts &k, const double *Sin, double *Sout,

@@ -1551,20 +1551,26 @@ static void stage_impl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
   // the FP32 form keeps its face states and fluxes in the same buffers, as floats
   float *SFf = (float *)b.SF, *FFf = (float *)b.FF, *UFf = (float *)b.UF;
   if (k.order == 2) {
-    if (f32) ffv_m5f_recon(m, g, k, b.S, SFf, b.status, st);
-    else m5_recon_face<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.status);
+    if (f32) {
+      // the FP32 copy of the state lives in RHS, which m5_cell_update writes later
+      ffv_m5f_shadow(m.n, k, b.S, (float *)b.RHS, st);
+      rec("m5f_shadow");
+      ffv_m5f_recon(m, g, k, b.S, (float *)b.RHS, SFf, b.status, st);
+    } else {
+      m5_recon_face<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.status);
+    }
     rec(f32 ? "m5f_recon_face" : k_names[0]);
   }
   if (f32) ffv_m5f_flux(m, g, k, b.S, SFf, FFf, UFf, b.GF, b.status, st);
   else m5_face_flux<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.FF, b.UF, b.GF, b.status);
   rec(f32 ? "m5f_face_flux" : k_names[1]);
   if (f32)
-    m5_cell_update<N, float><<<gc, tpb, 0, st>>>(m, g, k, b.S, b.SN, FFf, UFf, b.RHS, b.Snew,
-                                                 b.flag, b.dt, irk, b.status);
+    ffv_m5f_cell_update(m, g, k, b.S, b.SN, FFf, UFf, b.RHS, b.Snew, b.flag, b.dt, irk, b.status,
+                        st);
   else
     m5_cell_update<N, double><<<gc, tpb, 0, st>>>(m, g, k, b.S, b.SN, b.FF, b.UF, b.RHS, b.Snew,
                                                   b.flag, b.dt, irk, b.status);
-  rec(k_names[2]);
+  rec(f32 ? "m5f_cell_update" : k_names[2]);
   if (irk == 1) {
     flag_count<<<nb, CB, 0, st>>>(m.n, b.flag, b.bcount);
     rec(k_names[3]);
@@ -1599,5 +1605,6 @@ void ffv_m5_fp64_stage(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
 }
 
 int ffv_m5_launches_per_stage(const M5Consts &k, int irk) {
-  return (k.order == 2 ? 1 : 0) + 2 + (irk == 1 ? 4 : 0) + 1 + 4;
+  const int recon = k.order == 2 ? (k.precision == FFV_FP32_FLUX ? 2 : 1) : 0;
+  return recon + 2 + (irk == 1 ? 4 : 0) + 1 + 4;
 }
