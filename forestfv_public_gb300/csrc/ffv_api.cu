@@ -284,7 +284,16 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
       k.ig1[i] = gm1 != 0.0 ? 1.0 / gm1 : 0.0;
       k.gpg[i] = k.gpi[i] * k.ig1[i];
       k.igam[i] = p->gamma[i] != 0.0 ? 1.0 / p->gamma[i] : 0.0;
+      k.pinf_f[i] = (float)p->pinf[i];
+      k.igam_f[i] = (float)k.igam[i];
+      k.mu_f[i] = (float)p->mu[i];
+      k.gamma_f[i] = (float)p->gamma[i];
+      // m5_relaxationvec.c's floor -(1 - 1e-8) p_inf + 1e-8 and reset value
+      k.plo_f[i] = (float)(-(1.0 - 1.0e-8) * p->pinf[i] + 1.0e-8);
+      k.preset_f[i] = (float)(-(1.0 - 1.0e-8) * p->pinf[i] + 1.0);
     }
+    k.alo_f = (float)(p->amin / 100.0);
+    k.ahi_f = (float)(1.0 - (p->amin / 100.0));
   }
   int rc = FFV_OK;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||

@@ -15,6 +15,11 @@ struct M5Consts {
   // gamma p_inf / (gamma - 1), 1 / gamma
   double gpi[FFV_MAX_MATERIALS], ig1[FFV_MAX_MATERIALS], gpg[FFV_MAX_MATERIALS],
       igam[FFV_MAX_MATERIALS];
+  // the same in FP32: p_inf, 1 / gamma, mu, gamma, the relaxation's pressure floor and reset
+  // value, AMIN / 100 and 1 - AMIN / 100
+  float pinf_f[FFV_MAX_MATERIALS], igam_f[FFV_MAX_MATERIALS], mu_f[FFV_MAX_MATERIALS],
+      gamma_f[FFV_MAX_MATERIALS], plo_f[FFV_MAX_MATERIALS], preset_f[FFV_MAX_MATERIALS];
+  float alo_f, ahi_f;
 };
 
 struct ffv_m5_bufs {

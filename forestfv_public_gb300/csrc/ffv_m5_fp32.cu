@@ -143,8 +143,8 @@ __device__ void make_sol_f(const M5Consts &k, const float *U, double phi0, SolF<
   for (int i = 0; i < N; ++i) {
     const float press = U[RL::P + i];
     s.p[i] = press;
-    c2 += (s.avf[i] * ir) * (float)k.gamma[i] * (press + (float)k.pinf[i]);
-    eos_stress_f(s.st, s.avf[i], press, G, Gmag, (float)k.mu[i], nullptr);
+    c2 += (s.avf[i] * ir) * k.gamma_f[i] * (press + k.pinf_f[i]);
+    eos_stress_f(s.st, s.avf[i], press, G, Gmag, k.mu_f[i], nullptr);
   }
   s.c2 = c2;
 }
@@ -248,11 +248,11 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
   for (int v = 0; v < N; ++v) {
     const float rm = s.ra[v] / s.avf[v];
     const float rm_S = rm * (uK - SK) * ius;
-    const float ga = (float)k.gamma[v], pi = (float)k.pinf[v];
+    const float ga = k.gamma_f[v], pi = k.pinf_f[v];
     // the reference takes p_k = -p_hydro here (m5_star_region.c:122)
     const float p_S = (-s.p[v] + pi) * (((ga - 1.0f) * rm + (ga + 1.0f) * rm_S) /
                                        ((ga - 1.0f) * rm_S + (ga + 1.0f) * rm)) - pi;
-    const float ael = elastic_energy_f(G, Gmag, (float)k.mu[v]);
+    const float ael = elastic_energy_f(G, Gmag, k.mu_f[v]);
     const float eel = ael / (s.avf[v] * rm_S);
     const float e_S = (p_S + ga * pi) / (rm_S * (ga + 1.0f)) + eel;
     nc.are[v] = ar_S[v] * e_S;
@@ -431,7 +431,7 @@ __device__ unsigned relax_mixed(const M5Consts &k, double *V, double *avf_out, d
   gmat_f(A, G, Gmag);
   double ael[N];
 #pragma unroll
-  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, (float)k.mu[iv]);
+  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, k.mu_f[iv]);
   const double eps_sml = 1.0e-12, eps_big = 1.0e-8;
   unsigned st = 0;
   double ratio = 1.0;
@@ -501,11 +501,11 @@ __device__ unsigned relax_mixed(const M5Consts &k, double *V, double *avf_out, d
         if (avf[iv] > eps_sml) sum0 += avf[iv];
         a0[iv] = (float)avf[iv];
         pkf[iv] = (float)pkinit[iv];
-        pif[iv] = (float)k.pinf[iv];
+        pif[iv] = k.pinf_f[iv];
         b0[iv] = (float)(1.0 / (pkinit[iv] + k.pinf[iv]));
-        ig[iv] = (float)(1.0 / k.gamma[iv]);
-        plo[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + eps_big);
-        preset[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + 1.0);
+        ig[iv] = k.igam_f[iv];
+        plo[iv] = k.plo_f[iv];
+        preset[iv] = k.preset_f[iv];
         e[iv] = 0.0f;
       }
       const float F0 = (float)sum0;
@@ -644,7 +644,7 @@ __device__ void write_record(const M5Consts &k, const double *V, const double *p
     gmat_f(A, G, Gmag);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      const double ael = (double)elastic_energy_f(G, Gmag, (float)k.mu[i]);
+      const double ael = (double)elastic_energy_f(G, Gmag, k.mu_f[i]);
       const double p = ((k.gamma[i] - 1.0) * (V[C::i4 + i] - ael) / at[i]) - k.gamma[i] * k.pinf[i];
       out[(RL::P + i) * stride] = (float)p;
     }
@@ -672,7 +672,7 @@ __device__ __forceinline__ constexpr int crit_slot(int j) {
 template <int N>
 __device__ __forceinline__ void avf_limit_f(const M5Consts &k, float *S) {
   using C = K5<N>;
-  const float lo = (float)(k.amin / 100.0), hi = (float)(1.0 - (k.amin / 100.0));
+  const float lo = k.alo_f, hi = k.ahi_f;
   float sum = 0.0f;
 #pragma unroll
   for (int v = 0; v < N - 1; ++v) {
@@ -790,7 +790,7 @@ __device__ unsigned relax_face(const M5Consts &k, float *v, double *cr, double &
   float G[9], Gmag;
   gmat_f(v + C::i5, G, Gmag);
 #pragma unroll
-  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, (float)k.mu[iv]);
+  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, k.mu_f[iv]);
   const double eps_sml = 1.0e-12, eps_big = 1.0e-8;
   unsigned st = 0;
   float ratio = 1.0f;
@@ -845,12 +845,12 @@ __device__ unsigned relax_face(const M5Consts &k, float *v, double *cr, double &
         p0 += avf[iv] * pkinit[iv];
         a0[iv] = (float)avf[iv];
         pkf[iv] = (float)pkinit[iv];
-        pif[iv] = (float)k.pinf[iv];
+        pif[iv] = k.pinf_f[iv];
         // in FP64: at a material's pressure floor pk + p_inf is a few Pa beside 6e8
         b0[iv] = (float)(1.0 / (pkinit[iv] + k.pinf[iv]));
-        ig[iv] = (float)k.igam[iv];
-        plo[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + eps_big);
-        preset[iv] = (float)(-(1.0 - eps_big) * k.pinf[iv] + 1.0);
+        ig[iv] = k.igam_f[iv];
+        plo[iv] = k.plo_f[iv];
+        preset[iv] = k.preset_f[iv];
         e[iv] = 0.0f;
       }
       const float F0 = (float)sum0;
@@ -1235,10 +1235,10 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
     for (int j = 0; j < 3; j++) st_all[i][j] = 0.0f;
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    const float ael = elastic_energy_f(G, Gmag, (float)k.mu[i]);
+    const float ael = elastic_energy_f(G, Gmag, k.mu_f[i]);
     const double p = ((k.gamma[i] - 1.0) * (s[C::i4 + i] - (double)ael) / at[i]) - k.gpi[i];
     avf[i] = (float)at[i];
-    eos_stress_f(st_all, avf[i], (float)p, G, Gmag, (float)k.mu[i], ast[i]);
+    eos_stress_f(st_all, avf[i], (float)p, G, Gmag, k.mu_f[i], ast[i]);
   }
   double rhs[NA];
   float rhsA[9], nc[N - 1 + N + 9];
