@@ -34,6 +34,7 @@ SOURCES = {
     "ffv_noalloc.cu": [],
     "ffv_mlp.cu": [],
     "ffv_m0_tags.cu": [],
+    "ffv_adapt.cu": [],
 }
 
 

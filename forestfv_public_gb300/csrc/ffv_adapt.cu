@@ -1,0 +1,192 @@
+// Mesh adaptation: one refineh pass of the reference (refineh.c:3-57) on the owner-sorted
+// tables, with the state carried over on the device.
+//
+// Given each leaf's target level (ffv_tags), eight sibling leaves that all want a coarser
+// level merge into their parent, whose state is sum_k S_k / 8 in child order
+// (merge.c:35-45) followed, for model 5, by the pressure relaxation of the merged state
+// (merge.c:52-57); a leaf that wants a finer level splits into its eight children, which
+// copy its state (split.c:424-427); every other leaf is kept.  Merges and splits exclude
+// each other (all eight below their level vs. above it), so one sweep in leaf order does
+// both of the reference's loops.  The new leaves go through ffv_mesh_build; the context
+// then holds the new tables and the carried-over state.
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <unordered_map>
+#include <vector>
+
+#include "ffv_device.cuh"
+#include "ffv_m5.cuh"
+
+namespace {
+
+// new cell i takes old cell map[i] (>= 0) or the mean of old cells j..j+7 (map[i] = -1 - j)
+__global__ void adapt_remap(int64_t n_new, int64_t n_old, int neq, const int64_t *__restrict__ map,
+                            const double *__restrict__ Sold, double *__restrict__ Snew) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_new;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t src = map[i];
+    for (int v = 0; v < neq; v++) {
+      double x;
+      if (src >= 0) {
+        x = Sold[(int64_t)v * n_old + src];
+      } else {
+        const int64_t j = -1 - src;
+        x = 0.0;
+        for (int q = 0; q < 8; q++) x += Sold[(int64_t)v * n_old + j + q] / ((double)8);
+      }
+      Snew[(int64_t)v * n_new + i] = x;
+    }
+  }
+}
+
+}  // namespace
+
+// defined in ffv_api.cu
+int ffv_ctx_adapt_view(ffv_ctx *ctx, int *device, cudaStream_t *st, int64_t *n, int *neq,
+                       double **d_S, int *model, const M5Consts **k);
+extern "C" int ffv_set_mesh(ffv_ctx *c, const ffv_mesh *m);
+extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves, const int32_t *tree_ijk,
+                              const int32_t *level, const int32_t *cell_ijk, ffv_mesh **out,
+                              int64_t *order_out);
+extern "C" void ffv_mesh_free(ffv_mesh *m);
+int ffv_ctx_mark_state(ffv_ctx *ctx);
+
+extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **out) {
+  if (!ctx || !m || !split || !out) return FFV_ERR_ARG;
+  *out = nullptr;
+  int device, neq, model;
+  cudaStream_t st;
+  int64_t n;
+  double *d_S;
+  const M5Consts *k;
+  int rc = ffv_ctx_adapt_view(ctx, &device, &st, &n, &neq, &d_S, &model, &k);
+  if (rc != FFV_OK) return rc;
+  if (n != m->n) return FFV_ERR_ARG;
+  // sibling groups (tree, level, parent coordinates): member count and first member
+  struct Key {
+    uint64_t a, b;
+    bool operator==(const Key &o) const { return a == o.a && b == o.b; }
+  };
+  struct KeyHash {
+    size_t operator()(const Key &q) const {
+      return (size_t)(q.a * 0x9E3779B97F4A7C15ull ^ (q.b + 0x632BE59BD9B4E019ull + (q.a << 6)));
+    }
+  };
+  const uint64_t nt0 = (uint64_t)m->desc.ntrees[0], nt1 = (uint64_t)m->desc.ntrees[1];
+  auto key_of = [&](int64_t c, int l) {
+    const int32_t *t = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
+    const uint64_t tree = (uint64_t)t[0] + nt0 * ((uint64_t)t[1] + nt1 * (uint64_t)t[2]);
+    return Key{tree | ((uint64_t)l << 48), (uint64_t)(x[0] >> 1) | ((uint64_t)(x[1] >> 1) << 21) |
+                                               ((uint64_t)(x[2] >> 1) << 42)};
+  };
+  std::unordered_map<Key, std::pair<int64_t, int32_t>, KeyHash> groups;  // first, count
+  groups.reserve((size_t)n);
+  for (int64_t c = 0; c < n; c++) {
+    const int l = ffv_info_level(m->info[c]);
+    if (l <= 1) continue;
+    auto it = groups.find(key_of(c, l));
+    if (it == groups.end()) groups.emplace(key_of(c, l), std::make_pair(c, 1));
+    else it->second.second++;
+  }
+  std::vector<int32_t> tij, lev, cij;
+  std::vector<int64_t> map;
+  tij.reserve(3 * n);
+  lev.reserve(n);
+  cij.reserve(3 * n);
+  map.reserve(n);
+  int64_t nmerged = 0;
+  for (int64_t c = 0; c < n;) {
+    const int l = ffv_info_level(m->info[c]);
+    const int32_t *t = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
+    if (l > 1) {
+      const auto &g = groups.find(key_of(c, l))->second;
+      if (g.first == c && g.second == 8 && c + 8 <= n) {
+        bool all = true;
+        for (int q = 0; q < 8 && all; q++)
+          all = ffv_info_level(m->info[c + q]) == l && split[c + q] < l;
+        if (all) {  // merge.c: the parent of eight leaves
+          tij.insert(tij.end(), {t[0], t[1], t[2]});
+          lev.push_back(l - 1);
+          cij.insert(cij.end(), {x[0] >> 1, x[1] >> 1, x[2] >> 1});
+          map.push_back(-1 - c);
+          nmerged++;
+          c += 8;
+          continue;
+        }
+      }
+    }
+    if (split[c] > l) {  // split.c: eight children in child order, corner k at (bit1, bit0, bit2)
+      if (l + 1 > FFV_MAX_LEVEL) return FFV_ERR_TABLE;
+      for (int q = 0; q < 8; q++) {
+        tij.insert(tij.end(), {t[0], t[1], t[2]});
+        lev.push_back(l + 1);
+        cij.insert(cij.end(), {2 * x[0] + ((q >> 1) & 1), 2 * x[1] + (q & 1), 2 * x[2] + ((q >> 2) & 1)});
+        map.push_back(c);
+      }
+    } else {
+      tij.insert(tij.end(), {t[0], t[1], t[2]});
+      lev.push_back(l);
+      cij.insert(cij.end(), {x[0], x[1], x[2]});
+      map.push_back(c);
+    }
+    c++;
+  }
+  const int64_t n_new = (int64_t)lev.size();
+  ffv_mesh *nm = nullptr;
+  std::vector<int64_t> order(n_new);
+  rc = ffv_mesh_build(&m->desc, n_new, tij.data(), lev.data(), cij.data(), &nm, order.data());
+  if (rc != FFV_OK) return rc;
+  std::vector<int64_t> cmap(n_new);
+  for (int64_t j = 0; j < n_new; j++) cmap[j] = map[order[j]];
+  // carry the state over on the device, then swap the tables
+  cudaError_t e = cudaSetDevice(device);
+  int64_t *d_map = nullptr;
+  double *d_T = nullptr;
+  if (e == cudaSuccess) e = cudaMalloc(&d_map, sizeof(int64_t) * n_new);
+  if (e == cudaSuccess) e = cudaMalloc(&d_T, sizeof(double) * neq * n_new);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_map, cmap.data(), sizeof(int64_t) * n_new, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    adapt_remap<<<152 * 4, 256, 0, st>>>(n_new, n, neq, d_map, d_S, d_T);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess && model == 5 && nmerged > 0) {
+    ffv_m5_relax_merged(n_new, *k, d_map, d_T, st);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  rc = e == cudaSuccess ? FFV_OK : FFV_ERR_CUDA;
+  if (rc == FFV_OK) rc = ffv_set_mesh(ctx, nm);  // new tables and buffers; state unset
+  if (rc == FFV_OK) {
+    ffv_ctx_mark_state(ctx);
+    double *d_Snew = nullptr;
+    int64_t n2 = 0;
+    rc = ffv_ctx_adapt_view(ctx, &device, &st, &n2, &neq, &d_Snew, &model, &k);
+    if (rc == FFV_OK && (n2 != n_new || !d_Snew)) rc = FFV_ERR_STATE;
+    if (rc == FFV_OK) {
+      e = cudaMemcpyAsync(d_Snew, d_T, sizeof(double) * neq * n_new, cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) rc = FFV_ERR_CUDA;
+    }
+  }
+  cudaFree(d_map);
+  cudaFree(d_T);
+  if (rc != FFV_OK) {
+    ffv_mesh_free(nm);
+    return rc;
+  }
+  *out = nm;
+  return FFV_OK;
+}
+
+// the leaves of a mesh in its cell order (the inverse of ffv_mesh_build's input)
+extern "C" int ffv_mesh_leaves(const ffv_mesh *m, int32_t *tree_ijk, int32_t *level,
+                               int32_t *cell_ijk) {
+  if (!m || !tree_ijk || !level || !cell_ijk) return FFV_ERR_ARG;
+  memcpy(tree_ijk, m->tree_ijk, sizeof(int32_t) * 3 * m->n);
+  memcpy(cell_ijk, m->cell_ijk, sizeof(int32_t) * 3 * m->n);
+  for (int64_t c = 0; c < m->n; c++) level[c] = ffv_info_level(m->info[c]);
+  return FFV_OK;
+}

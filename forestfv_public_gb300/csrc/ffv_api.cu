@@ -215,6 +215,27 @@ int ffv_ctx_view(ffv_ctx *c, int *device, cudaStream_t *st, ffv_dmesh *dm, const
   return FFV_OK;
 }
 
+// the context's state for ffv_adapt (ffv_adapt.cu)
+int ffv_ctx_adapt_view(ffv_ctx *c, int *device, cudaStream_t *st, int64_t *n, int *neq,
+                       double **d_S, int *model, const M5Consts **k) {
+  if (!c) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  *device = c->device;
+  *st = c->stream;
+  *n = c->n;
+  *neq = c->neq;
+  *d_S = c->d_S;
+  *model = c->p.model;
+  *k = &c->m5;
+  return FFV_OK;
+}
+
+int ffv_ctx_mark_state(ffv_ctx *c) {
+  if (!c || !c->have_mesh) return FFV_ERR_STATE;
+  c->have_state = 1;
+  return FFV_OK;
+}
+
 extern "C" {
 
 const char *ffv_error_string(int code) {

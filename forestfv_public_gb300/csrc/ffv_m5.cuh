@@ -83,3 +83,7 @@ void ffv_m0_tags(const ffv_dmesh &m, double gamma, double pinf, const ffv_m5_tag
                  const double *S, int32_t *split, cudaStream_t st);
 void ffv_m0_indicator_fields(int64_t n, double gamma, double pinf, const double *S, float *F,
                              cudaStream_t st);
+
+// the reference's FP64 relaxation of the cells a mesh adaptation merged (map < 0)
+void ffv_m5_relax_merged(int64_t n, const M5Consts &k, const int64_t *map, double *S,
+                         cudaStream_t st);

@@ -1485,7 +1485,30 @@ __global__ void __launch_bounds__(128) m5_indicator_fields(int64_t n, M5Consts k
   F[4 * n + c] = (float)sqrt(1.5 * j2);
 }
 
+// merged cells of a mesh adaptation (map < 0): the reference's relaxation of the merged
+// state (merge.c:52-57)
+template <int N>
+__global__ void __launch_bounds__(128) m5_relax_merged(int64_t n, M5Consts k,
+                                                       const int64_t *__restrict__ map,
+                                                       double *__restrict__ S) {
+  using C = K5<N>;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n || map[c] >= 0) return;
+  double s[C::NEQ];
+  load_state<N>(S, n, c, s);
+  relaxationvec<N>(k, s);
+#pragma unroll
+  for (int e = 0; e < C::NEQ; e++) S[(int64_t)e * n + c] = s[e];
+}
+
 }  // namespace
+
+void ffv_m5_relax_merged(int64_t n, const M5Consts &k, const int64_t *map, double *S,
+                         cudaStream_t st) {
+  const unsigned gc = (unsigned)((n + 127) / 128);
+  if (k.nmat == 2) m5_relax_merged<2><<<gc, 128, 0, st>>>(n, k, map, S);
+  else m5_relax_merged<3><<<gc, 128, 0, st>>>(n, k, map, S);
+}
 
 void ffv_m5_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
                              cudaStream_t st) {

@@ -97,6 +97,22 @@ class Mesh:
         self.tree_ijk = tij[self.order]
         self.cell_ijk = cij[self.order]
 
+    @classmethod
+    def from_handle(cls, h, ntrees, bc, tree_edge) -> "Mesh":
+        """Wrap tables the library built itself (ffv_adapt)."""
+        L = _lib.lib()
+        m = cls.__new__(cls)
+        m.ntrees, m.bc, m.tree_edge = tuple(ntrees), tuple(bc), float(tree_edge)
+        m._h = h
+        m.n = int(L.ffv_mesh_ncells(h))
+        m.tree_ijk = np.empty((m.n, 3), np.int32)
+        m.cell_ijk = np.empty((m.n, 3), np.int32)
+        m.level = np.empty(m.n, np.int32)
+        _lib.check(L.ffv_mesh_leaves(h, m.tree_ijk.ctypes.data, m.level.ctypes.data,
+                                     m.cell_ijk.ctypes.data), "ffv_mesh_leaves")
+        m.order = np.arange(m.n, dtype=np.int64)
+        return m
+
     @property
     def handle(self):
         return self._h

@@ -90,6 +90,29 @@ class Solver:
                                        si.ctypes.data if with_raw else None), "ffv_tags")
         return (split, raw, si) if with_raw else split
 
+    def adapt(self, split) -> Mesh:
+        """One refineh pass (ffv_adapt) with target levels `split`; the solver continues on
+        the returned mesh with the carried-over state."""
+        split = np.ascontiguousarray(split, dtype=np.int32)
+        assert split.shape == (self.mesh.n,)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().ffv_adapt(self._h, self.mesh.handle, split.ctypes.data,
+                                        ctypes.byref(h)), "ffv_adapt")
+        old = self.mesh
+        self.mesh = Mesh.from_handle(h, old.ntrees, old.bc, old.tree_edge)
+        return self.mesh
+
+    def meshadaptation(self, params) -> Mesh:
+        """The reference's meshadaptation (meshadaptation.c:3-46): LEVEL + 1 rounds of the
+        refinement tags and one refineh pass, LEVEL the largest level the criteria name."""
+        if not isinstance(params, _lib.TagParams):
+            params = _lib.TagParams.from_tuple(params)
+        level = max(params.lvl_uniform, params.lvl_prs, params.lvl_rho, params.lvl_vel,
+                    params.lvl_inter0, params.lvl_inter1)
+        for _ in range(level + 1):
+            self.adapt(self.tags(params))
+        return self.mesh
+
     def cfl_dt(self, cfl: float) -> float:
         out = ctypes.c_double()
         _lib.check(_lib.lib().ffv_cfl_dt(self._h, cfl, ctypes.byref(out)), "ffv_cfl_dt")

@@ -183,6 +183,16 @@ int ffv_tags(ffv_ctx *ctx, const ffv_mesh *m, const ffv_tag_params *p, int32_t *
 /* criterionsmth alone, in place on split[n] (host): level_max is the reference's LEVEL,
  * the largest level any criterion names. */
 int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *split);
+/* One refineh pass (refineh.c:3-57, merge.c, split.c): with split[n] the target levels of
+ * the leaves of `m` (the mesh set on the context), eight sibling leaves that all want a
+ * coarser level merge (state: the mean of the eight, then for model 5 the reference's
+ * pressure relaxation), a leaf that wants a finer level splits into eight children with
+ * its state, the rest stay.  *out receives the new mesh (ffv_mesh_free); the context holds
+ * its tables and the carried-over state.  The reference's meshadaptation is LEVEL + 1 rounds
+ * of ffv_tags + ffv_adapt. */
+int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **out);
+/* The leaves of a mesh in its cell order (tree_ijk[3n], level[n], cell_ijk[3n]). */
+int ffv_mesh_leaves(const ffv_mesh *m, int32_t *tree_ijk, int32_t *level, int32_t *cell_ijk);
 
 /* Learned refinement indicator (no counterpart in the reference): a 135-64-64-1
  * perceptron with GELU hidden layers and a sigmoid output over the 27-cell stencil of five

@@ -118,8 +118,9 @@ void __wrap_m0_init_domain(struct RUN *run) {
 /* <case>.rf:  sphere cx cy cz r level_inside level_outside
  *             box x0 y0 z0 x1 y1 z1 level_inside level_outside */
 void __real_criterionsplt(struct RUN *run);
+static int g_real_criterion = 0; /* set while the harness runs the reference's adaptation */
 void __wrap_criterionsplt(struct RUN *run) {
-  FILE *fp = open_case_file(run, ".rf");
+  FILE *fp = g_real_criterion ? NULL : open_case_file(run, ".rf");
   if (!fp) { __real_criterionsplt(run); return; }
   char kind[64];
   double a[8] = {0};
@@ -202,6 +203,47 @@ static void dump(struct RUN *run, const char *tag, double loop_seconds, int64_t 
  * criterionsplt recompute SI and split for every leaf).  Output <run>.tags.bin: "FFVT",
  * npass, n, then per pass and leaf SI[0], SI[1], the split level criterionsplt gives and
  * the split level after criterionsmth. */
+/* set the reference's criterion globals from one .tag/.adapt line (values as the input
+ * file gives them), deriving the rest as inputset.c:106 and m5_input.c:50-57 do */
+static int set_criteria(FILE *fp) {
+  int u, lu, pr, lp, rh, lr, ve, lv, i0, l0, r0, i1, l1, r1;
+  double tp, tr, tv;
+  if (fscanf(fp, "%d %d %d %d %lf %d %d %lf %d %d %lf %d %d %d %d %d %d", &u, &lu, &pr, &lp, &tp,
+             &rh, &lr, &tr, &ve, &lv, &tv, &i0, &l0, &r0, &i1, &l1, &r1) != 17)
+    return 0;
+  CRT_UNIFORM = u; CRT_LVL_UNIFORM = lu;
+  CRT_GEO_AREA = 0; CRT_LVL_GEO_AREA = 0;
+  CRT_GRAD_PRS = pr; CRT_LVL_GRAD_PRS = lp; CRT_GRAD_PRS_THR = tp;
+  CRT_GRAD_RHO = rh; CRT_LVL_GRAD_RHO = lr; CRT_GRAD_RHO_THR = tr;
+  CRT_GRAD_VEL = ve; CRT_LVL_GRAD_VEL = lv; CRT_GRAD_VEL_THR = tv;
+  CRT_ADAPT_INTER_0 = i0; CRT_LVL_ADAPT_INTER_0 = l0; CRT_LRS_ADAPT_INTER_0 = r0;
+  CRT_ADAPT_INTER_1 = i1; CRT_LVL_ADAPT_INTER_1 = l1; CRT_LRS_ADAPT_INTER_1 = r0 + r1;
+  ADAPT_INTER_MAX = 0;
+  if (i0 == 1 && i1 == 1) ADAPT_INTER_MAX = CRT_LRS_ADAPT_INTER_0 + CRT_LRS_ADAPT_INTER_1;
+  if (i0 == 1 && i1 == 0) ADAPT_INTER_MAX = CRT_LRS_ADAPT_INTER_0;
+  LEVEL = max(max(max(max(lu, 0), lp), lr), lv);
+  LEVEL = max(max(LEVEL, l0), l1);
+  return 1;
+}
+
+/* <case>.adapt: one criterion line; after the loop (and the tag passes) the reference's own
+ * meshadaptation (meshadaptation.c:3-46: LEVEL+1 passes of criterionsplt, criterionsmth,
+ * refineh, restructtopo, meshproperties, interface_location) runs on the final state and
+ * the adapted leaf list is dumped as <run>.adapt.bin */
+static void adapt_pass(struct RUN *run) {
+  FILE *fp = open_case_file(run, ".adapt");
+  if (!fp) return;
+  int ok = set_criteria(fp);
+  fclose(fp);
+  if (!ok) { fprintf(stderr, "harness: bad .adapt\n"); exit(3); }
+  for (struct BRANCH *c = run->topo->locl; c; c = c->lnxt) c->el->SI[0] = c->el->SI[1] = 0;
+  if (CRT_ADAPT_INTER_0 != 0) interface_location(run);
+  g_real_criterion = 1;
+  meshadaptation(run);
+  g_real_criterion = 0;
+  dump(run, "adapt", 0.0, 0);
+}
+
 static void tag_pass(struct RUN *run) {
   FILE *fp = open_case_file(run, ".tag");
   if (!fp) return;
@@ -260,6 +302,7 @@ void __wrap_loop(struct RUN *run) {
   double t1 = MPI_Wtime();
   dump(run, "final", t1 - t0, (int64_t)NSTEP + 1);
   tag_pass(run);
+  adapt_pass(run);
 }
 
 /* m5_init_domain.c does not compile as published; this replacement assigns each leaf one

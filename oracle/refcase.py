@@ -100,6 +100,9 @@ class Case:
     # per pass: (uniform, lvl, prs, lvl, thr, rho, lvl, thr, vel, lvl, thr, inter0, lvl,
     # lrs, inter1, lvl, lrs) as the reference's input file gives them
     tags: tuple | None = None
+    # criteria of the reference's own meshadaptation run on the final state (harness
+    # .adapt file); the adapted leaf list comes back as the third dump
+    adapt: tuple | None = None
 
     @property
     def neq(self) -> int:
@@ -204,6 +207,10 @@ def write_case(c: Case, d: str, name: str = "case") -> str:
             for t in c.tags:
                 f.write(" ".join(repr(float(v)) if isinstance(v, float) else str(int(v))
                                  for v in t) + "\n")
+    if c.adapt is not None:
+        with open(base + ".adapt", "w") as f:
+            f.write(" ".join(repr(float(v)) if isinstance(v, float) else str(int(v))
+                             for v in c.adapt) + "\n")
     if c.m5 and c.m5.get("mix"):
         with open(base + ".mix", "w") as f:
             f.write(c.m5["mix"] + "\n")
@@ -234,6 +241,7 @@ class Dump:
     dist_cc: np.ndarray
     S: np.ndarray
     tags: np.ndarray | None = None  # [npass, n, 4]: SI[0], SI[1], split, smoothed split
+    adapted: "Dump | None" = None  # the leaf list after the reference's meshadaptation
 
 
 _LEAF_HDR = struct.Struct("<2i16i3dd2i")
@@ -290,6 +298,8 @@ def run_case(c: Case, workdir: str | None = None, timeout: float = 600.0):
             npass, n = struct.unpack_from("<2i", buf, 4)
             final.tags = np.frombuffer(buf, dtype="<i4", count=4 * n * npass,
                                        offset=12).reshape(npass, n, 4).copy()
+        if os.path.exists(run + ".adapt.bin"):
+            final.adapted = read_dump(run + ".adapt.bin")
         return read_dump(run + ".init.bin"), final, r.stdout
     finally:
         if own:

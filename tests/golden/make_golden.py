@@ -88,6 +88,14 @@ TAG_PASSES = (
 )
 
 
+# the reference's meshadaptation on the final state of these cases (same criterion order)
+ADAPT = {
+    "m5_bubble_prelax3": (1, 2, 0, 0, 0.0, 1, 5, 0.05, 0, 0, 0.0, 0, 0, 0, 0, 0, 0),
+    "m5_mild_prelax1": (1, 2, 1, 4, 0.2, 1, 4, 0.1, 0, 0, 0.0, 1, 4, 1, 0, 0, 0),
+    "m5_wall_amr": (1, 2, 1, 4, 0.2, 1, 4, 0.1, 0, 0, 0.0, 1, 4, 1, 0, 0, 0),
+}
+
+
 def config1_case() -> rc.Case:
     """Plain-method Sod problem of the 32^3 uniform forest: 4^3 trees at level 4, ideal
     gas, transmissive, MUSCL-HLLC, RK_STEPS 2, 100 steps.  The reference has no CFL
@@ -114,6 +122,10 @@ def save(name: str, c: rc.Case, keep_geom: bool) -> None:
     if final.tags is not None:
         d["tag_params"] = np.asarray(c.tags, dtype=np.float64)
         d["tags"] = final.tags.astype(np.int8)
+    if final.adapted is not None:
+        a = final.adapted
+        d.update(adapt_params=np.asarray(c.adapt, dtype=np.float64), adapt_root=a.root,
+                 adapt_level=a.level, adapt_adrs=a.adrs.astype(np.int8), adapt_S=a.S)
     if keep_geom:
         d.update(bc=final.bc.astype(np.int8), nn=final.nneig.astype(np.int8),
                  neigfc=final.neigfc.astype(np.int8), nb=final.nb, area=final.area,
@@ -131,6 +143,7 @@ def main() -> None:
         save(name, c, g)
     for name, c in M5_CASES.items():
         c.tags = TAG_PASSES
+        c.adapt = ADAPT.get(name)
         save(name, c, True)
     save("m0_config1_sod32", config1_case(), False)
 
