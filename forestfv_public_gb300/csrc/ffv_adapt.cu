@@ -13,7 +13,6 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include <unordered_map>
 #include <vector>
 
 #include "ffv_device.cuh"
@@ -64,32 +63,6 @@ extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, 
   int rc = ffv_ctx_adapt_view(ctx, &device, &st, &n, &neq, &d_S, &model, &k);
   if (rc != FFV_OK) return rc;
   if (n != m->n) return FFV_ERR_ARG;
-  // sibling groups (tree, level, parent coordinates): member count and first member
-  struct Key {
-    uint64_t a, b;
-    bool operator==(const Key &o) const { return a == o.a && b == o.b; }
-  };
-  struct KeyHash {
-    size_t operator()(const Key &q) const {
-      return (size_t)(q.a * 0x9E3779B97F4A7C15ull ^ (q.b + 0x632BE59BD9B4E019ull + (q.a << 6)));
-    }
-  };
-  const uint64_t nt0 = (uint64_t)m->desc.ntrees[0], nt1 = (uint64_t)m->desc.ntrees[1];
-  auto key_of = [&](int64_t c, int l) {
-    const int32_t *t = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
-    const uint64_t tree = (uint64_t)t[0] + nt0 * ((uint64_t)t[1] + nt1 * (uint64_t)t[2]);
-    return Key{tree | ((uint64_t)l << 48), (uint64_t)(x[0] >> 1) | ((uint64_t)(x[1] >> 1) << 21) |
-                                               ((uint64_t)(x[2] >> 1) << 42)};
-  };
-  std::unordered_map<Key, std::pair<int64_t, int32_t>, KeyHash> groups;  // first, count
-  groups.reserve((size_t)n);
-  for (int64_t c = 0; c < n; c++) {
-    const int l = ffv_info_level(m->info[c]);
-    if (l <= 1) continue;
-    auto it = groups.find(key_of(c, l));
-    if (it == groups.end()) groups.emplace(key_of(c, l), std::make_pair(c, 1));
-    else it->second.second++;
-  }
   std::vector<int32_t> tij, lev, cij;
   std::vector<int64_t> map;
   tij.reserve(3 * n);
@@ -100,12 +73,10 @@ extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, 
   for (int64_t c = 0; c < n;) {
     const int l = ffv_info_level(m->info[c]);
     const int32_t *t = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
-    if (l > 1) {
-      const auto &g = groups.find(key_of(c, l))->second;
-      if (g.first == c && g.second == 8 && c + 8 <= n) {
+    if (l > 1 && ffv_sibling_group(m, c) == c) {
+      {
         bool all = true;
-        for (int q = 0; q < 8 && all; q++)
-          all = ffv_info_level(m->info[c + q]) == l && split[c + q] < l;
+        for (int q = 0; q < 8 && all; q++) all = split[c + q] < l;
         if (all) {  // merge.c: the parent of eight leaves
           tij.insert(tij.end(), {t[0], t[1], t[2]});
           lev.push_back(l - 1);

@@ -48,6 +48,13 @@ struct ffv_level_geom {
   double inv_unused;
 };
 
+// first cell of the complete group of eight sibling leaves that holds cell c, or -1 when
+// some sibling is not a leaf (then the group is not in the table).  In the tables' cell
+// order (depth-first by child index) the eight children of a parent are consecutive, and
+// child k of a parent sits at cell coordinates 2p + (bit1 k, bit0 k, bit2 k).
+struct ffv_mesh;
+int64_t ffv_sibling_group(const ffv_mesh *m, int64_t c);
+
 struct ffv_mesh {
   ffv_forest_desc desc;
   int64_t n;

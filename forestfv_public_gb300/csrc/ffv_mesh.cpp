@@ -15,7 +15,7 @@
 
 #include <algorithm>
 #include <new>
-#include <unordered_map>
+#include <thread>
 #include <vector>
 
 #include "ffv_internal.h"
@@ -122,6 +122,63 @@ uint64_t cell_key(int level, uint32_t gx, uint32_t gy, uint32_t gz) {
   return ((uint64_t)level << 60) | morton(gx, gy, gz);
 }
 
+// fn(t, c0, c1) over [0, n) in nthreads contiguous chunks, on nthreads host threads
+template <typename Fn>
+void parallel_chunks(int64_t n, int nthreads, Fn fn) {
+  const int64_t chunk = (n + nthreads - 1) / nthreads;
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; t++)
+    pool.emplace_back([&, t] { fn(t, std::min(n, t * chunk), std::min(n, (t + 1) * chunk)); });
+  fn(0, 0, std::min(n, chunk));
+  for (auto &th : pool) th.join();
+}
+
+int host_threads() {
+  return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+}
+
+// open-addressing map from cell keys to cell indices (linear probing, power-of-two size;
+// filled once, then only read -- from several threads)
+struct CellMap {
+  std::vector<uint64_t> keys;
+  std::vector<int32_t> vals;  // -1: empty slot
+  uint64_t mask = 0;
+  CellMap(int64_t n, int nthreads) {
+    uint64_t cap = 16;
+    while (cap < (uint64_t)(2 * n)) cap <<= 1;
+    keys.resize(cap);
+    vals.resize(cap);
+    mask = cap - 1;
+    parallel_chunks((int64_t)cap, nthreads, [&](int, int64_t a, int64_t b) {
+      for (int64_t i = a; i < b; i++) vals[i] = -1;
+    });
+  }
+  static uint64_t mix(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+  }
+  // insert a key known to be absent (keys are distinct: overlapping leaves are rejected
+  // before); safe from several threads at once -- a slot is claimed by an atomic
+  // compare-and-swap of its value, and the table is only read after all inserts
+  void put_new(uint64_t k, int32_t v) {
+    for (uint64_t i = mix(k) & mask;; i = (i + 1) & mask) {
+      int32_t expect = -1;
+      if (__atomic_compare_exchange_n(&vals[i], &expect, v, false, __ATOMIC_RELAXED,
+                                      __ATOMIC_RELAXED)) {
+        keys[i] = k;
+        return;
+      }
+    }
+  }
+  int32_t get(uint64_t k) const {
+    for (uint64_t i = mix(k) & mask;; i = (i + 1) & mask) {
+      if (vals[i] < 0) return -1;
+      if (keys[i] == k) return vals[i];
+    }
+  }
+};
+
 }  // namespace
 
 extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
@@ -137,39 +194,56 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
   for (int s = 0; s < 6; s++)
     if (desc->bc[s] < 1 || desc->bc[s] > 5) return FFV_ERR_ARG;
 
-  int lmin = FFV_MAX_LEVEL, lmax = 1;
-  for (int64_t i = 0; i < nleaves; i++) {
-    int l = level[i];
-    if (l < 1 || l > FFV_MAX_LEVEL) return FFV_ERR_TABLE;
-    lmin = std::min(lmin, l);
-    lmax = std::max(lmax, l);
-    const int32_t ext = 1 << (l - 1);
-    for (int a = 0; a < 3; a++) {
-      if (tree_ijk[3 * i + a] < 0 || tree_ijk[3 * i + a] >= T[a]) return FFV_ERR_TABLE;
-      if (cell_ijk[3 * i + a] < 0 || cell_ijk[3 * i + a] >= ext) return FFV_ERR_TABLE;
+  const int nthreads = host_threads();
+  std::vector<int> tmin(nthreads, FFV_MAX_LEVEL), tmax(nthreads, 1), terr(nthreads, FFV_OK);
+  parallel_chunks(nleaves, nthreads, [&](int t, int64_t c0, int64_t c1) {
+    for (int64_t i = c0; i < c1 && terr[t] == FFV_OK; i++) {
+      int l = level[i];
+      if (l < 1 || l > FFV_MAX_LEVEL) {
+        terr[t] = FFV_ERR_TABLE;
+        break;
+      }
+      tmin[t] = std::min(tmin[t], l);
+      tmax[t] = std::max(tmax[t], l);
+      const int32_t ext = 1 << (l - 1);
+      for (int a = 0; a < 3; a++)
+        if (tree_ijk[3 * i + a] < 0 || tree_ijk[3 * i + a] >= T[a] || cell_ijk[3 * i + a] < 0 ||
+            cell_ijk[3 * i + a] >= ext)
+          terr[t] = FFV_ERR_TABLE;
+      // global coordinates at the leaf level must fit the 21-bit Morton lanes
+      if (terr[t] == FFV_OK && ((int64_t)T[0] * ext > (1 << 21) || (int64_t)T[1] * ext > (1 << 21) ||
+                                (int64_t)T[2] * ext > (1 << 21)))
+        terr[t] = FFV_ERR_UNSUPPORTED;
     }
-    // global coordinates at the leaf level must fit the 21-bit Morton lanes
-    if ((int64_t)T[0] * ext > (1 << 21) || (int64_t)T[1] * ext > (1 << 21) ||
-        (int64_t)T[2] * ext > (1 << 21))
-      return FFV_ERR_UNSUPPORTED;
+  });
+  int lmin = FFV_MAX_LEVEL, lmax = 1;
+  for (int t = 0; t < nthreads; t++) {
+    if (terr[t] != FFV_OK) return terr[t];
+    lmin = std::min(lmin, tmin[t]);
+    lmax = std::max(lmax, tmax[t]);
   }
   const int D = lmax - 1;  // local depth of the finest leaves
 
   // canonical order: trees by Morton key of their indices, then depth-first by child index
   std::vector<int64_t> perm(nleaves);
   std::vector<uint64_t> tkey(nleaves), lkey(nleaves);
-  for (int64_t i = 0; i < nleaves; i++) {
-    perm[i] = i;
-    tkey[i] = morton(tree_ijk[3 * i], tree_ijk[3 * i + 1], tree_ijk[3 * i + 2]);
-    int sh = D - (level[i] - 1);
-    lkey[i] = morton((uint32_t)cell_ijk[3 * i] << sh, (uint32_t)cell_ijk[3 * i + 1] << sh,
-                     (uint32_t)cell_ijk[3 * i + 2] << sh);
-  }
-  std::sort(perm.begin(), perm.end(), [&](int64_t a, int64_t b) {
+  parallel_chunks(nleaves, nthreads, [&](int, int64_t c0, int64_t c1) {
+    for (int64_t i = c0; i < c1; i++) {
+      perm[i] = i;
+      tkey[i] = morton(tree_ijk[3 * i], tree_ijk[3 * i + 1], tree_ijk[3 * i + 2]);
+      int sh = D - (level[i] - 1);
+      lkey[i] = morton((uint32_t)cell_ijk[3 * i] << sh, (uint32_t)cell_ijk[3 * i + 1] << sh,
+                       (uint32_t)cell_ijk[3 * i + 2] << sh);
+    }
+  });
+  auto before = [&](int64_t a, int64_t b) {
     if (tkey[a] != tkey[b]) return tkey[a] < tkey[b];
     if (lkey[a] != lkey[b]) return lkey[a] < lkey[b];
     return level[a] < level[b];
-  });
+  };
+  bool sorted = true;  // leaves given in canonical order (a regrid's output) need no sort
+  for (int64_t i = 0; i + 1 < nleaves && sorted; i++) sorted = !before(i + 1, i);
+  if (!sorted) std::sort(perm.begin(), perm.end(), before);
   // overlap check: a leaf's key range must end before the next leaf of the same tree starts
   for (int64_t k = 0; k + 1 < nleaves; k++) {
     int64_t a = perm[k], b = perm[k + 1];
@@ -230,89 +304,128 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
     }
   }
 
-  std::unordered_map<uint64_t, int32_t> where;
-  where.reserve((size_t)nleaves * 2);
+  CellMap where(nleaves, nthreads);
   std::vector<uint32_t> gx(3 * nleaves);
-  for (int64_t c = 0; c < nleaves; c++) {
-    int64_t i = perm[c];
-    if (order_out) order_out[c] = i;
-    for (int a = 0; a < 3; a++) {
-      m->tree_ijk[3 * c + a] = tree_ijk[3 * i + a];
-      m->cell_ijk[3 * c + a] = cell_ijk[3 * i + a];
-      gx[3 * c + a] = (uint32_t)tree_ijk[3 * i + a] * (1u << (level[i] - 1)) +
-                      (uint32_t)cell_ijk[3 * i + a];
+  const int64_t chunk = (nleaves + nthreads - 1) / nthreads;
+  auto fill = [&](int t) {
+    const int64_t c0 = t * chunk, c1 = std::min<int64_t>(nleaves, c0 + chunk);
+    for (int64_t c = c0; c < c1; c++) {
+      int64_t i = perm[c];
+      if (order_out) order_out[c] = i;
+      for (int a = 0; a < 3; a++) {
+        m->tree_ijk[3 * c + a] = tree_ijk[3 * i + a];
+        m->cell_ijk[3 * c + a] = cell_ijk[3 * i + a];
+        gx[3 * c + a] = (uint32_t)tree_ijk[3 * i + a] * (1u << (level[i] - 1)) +
+                        (uint32_t)cell_ijk[3 * i + a];
+      }
+      where.put_new(cell_key(level[i], gx[3 * c], gx[3 * c + 1], gx[3 * c + 2]), (int32_t)c);
     }
-    where[cell_key(level[i], gx[3 * c], gx[3 * c + 1], gx[3 * c + 2])] = (int32_t)c;
+  };
+  {
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; t++) pool.emplace_back(fill, t);
+    fill(0);
+    for (auto &th : pool) th.join();
   }
 
-  std::vector<int32_t> sub;
-  int rc = FFV_OK;
-  for (int64_t c = 0; c < nleaves && rc == FFV_OK; c++) {
-    int l = level[perm[c]];
-    uint32_t info = (uint32_t)l << 24;
-    for (int f = 0; f < 6; f++) {
-      const ffv_face_frame &fr = m->frame[f];
-      int a = fr.side_axis;
-      int64_t g[3] = {gx[3 * c], gx[3 * c + 1], gx[3 * c + 2]};
-      g[a] += fr.side_dir;
-      int64_t ext = (int64_t)T[a] << (l - 1);
-      uint32_t kind;
-      int32_t slot = -1;
-      if (g[a] < 0 || g[a] >= ext) {
-        int side = 2 * a + (fr.side_dir > 0 ? 1 : 0);
-        kind = FFV_FK_BC | (uint32_t)desc->bc[side];
-      } else {
-        auto it = where.find(cell_key(l, (uint32_t)g[0], (uint32_t)g[1], (uint32_t)g[2]));
-        if (it != where.end()) {
-          kind = FFV_FK_SAME;
-          slot = it->second;
-        } else if (l > 1 && (it = where.find(cell_key(l - 1, (uint32_t)(g[0] >> 1),
-                                                     (uint32_t)(g[1] >> 1),
-                                                     (uint32_t)(g[2] >> 1)))) != where.end()) {
-          kind = FFV_FK_COARSER;
-          slot = it->second;
+  // face tables, in the same chunks; subface groups are numbered per chunk and shifted
+  // afterwards, which gives the numbering of one sweep in cell order
+  std::vector<std::vector<int32_t>> csub(nthreads);
+  std::vector<int> crc(nthreads, FFV_OK);
+  auto work = [&](int t) {
+    const int64_t c0 = t * chunk, c1 = std::min<int64_t>(nleaves, c0 + chunk);
+    std::vector<int32_t> &sub = csub[t];
+    for (int64_t c = c0; c < c1; c++) {
+      int l = level[perm[c]];
+      uint32_t info = (uint32_t)l << 24;
+      for (int f = 0; f < 6; f++) {
+        const ffv_face_frame &fr = m->frame[f];
+        int a = fr.side_axis;
+        int64_t g[3] = {gx[3 * c], gx[3 * c + 1], gx[3 * c + 2]};
+        g[a] += fr.side_dir;
+        int64_t ext = (int64_t)T[a] << (l - 1);
+        uint32_t kind;
+        int32_t slot = -1;
+        if (g[a] < 0 || g[a] >= ext) {
+          int side = 2 * a + (fr.side_dir > 0 ? 1 : 0);
+          kind = FFV_FK_BC | (uint32_t)desc->bc[side];
         } else {
-          // four finer neighbours; subface k touches node ffv_face_nodes[f][k] of this face
-          int32_t ids[4];
-          bool ok = l < FFV_MAX_LEVEL;
-          for (int k = 0; k < 4 && ok; k++) {
-            int q = ffv_face_nodes[f][k];
-            int cb[3] = {ffv_corner_x(q), ffv_corner_y(q), ffv_corner_z(q)};
-            uint32_t fg[3];
-            for (int b = 0; b < 3; b++)
-              fg[b] = (uint32_t)(2 * g[b] + (b == a ? (fr.side_dir > 0 ? 0 : 1) : cb[b]));
-            auto jt = where.find(cell_key(l + 1, fg[0], fg[1], fg[2]));
-            if (jt == where.end()) ok = false; else ids[k] = jt->second;
-          }
-          if (!ok) {
-            // distinguish a 2:1 violation (deeper leaves behind the face) from a hole
-            bool deeper = false;
-            for (int d = 2; d + l <= FFV_MAX_LEVEL && !deeper; d++) {
+          int32_t hit = where.get(cell_key(l, (uint32_t)g[0], (uint32_t)g[1], (uint32_t)g[2]));
+          if (hit >= 0) {
+            kind = FFV_FK_SAME;
+            slot = hit;
+          } else if (l > 1 && (hit = where.get(cell_key(l - 1, (uint32_t)(g[0] >> 1),
+                                                        (uint32_t)(g[1] >> 1),
+                                                        (uint32_t)(g[2] >> 1)))) >= 0) {
+            kind = FFV_FK_COARSER;
+            slot = hit;
+          } else {
+            // four finer neighbours; subface k touches node ffv_face_nodes[f][k] of this face
+            int32_t ids[4];
+            bool ok = l < FFV_MAX_LEVEL;
+            for (int k = 0; k < 4 && ok; k++) {
+              int q = ffv_face_nodes[f][k];
+              int cb[3] = {ffv_corner_x(q), ffv_corner_y(q), ffv_corner_z(q)};
               uint32_t fg[3];
               for (int b = 0; b < 3; b++)
-                fg[b] = (uint32_t)((g[b] << d) + (b == a ? (fr.side_dir > 0 ? 0 : (1 << d) - 1) : 0));
-              deeper = where.count(cell_key(l + d, fg[0], fg[1], fg[2])) > 0;
+                fg[b] = (uint32_t)(2 * g[b] + (b == a ? (fr.side_dir > 0 ? 0 : 1) : cb[b]));
+              ids[k] = where.get(cell_key(l + 1, fg[0], fg[1], fg[2]));
+              ok = ids[k] >= 0;
             }
-            bool coarser = false;
-            for (int d = 2; l - d >= 1 && !coarser; d++)
-              coarser = where.count(cell_key(l - d, (uint32_t)(g[0] >> d), (uint32_t)(g[1] >> d),
-                                             (uint32_t)(g[2] >> d))) > 0;
-            rc = (deeper || coarser) ? FFV_ERR_BALANCE : FFV_ERR_TABLE;
-            break;
+            if (!ok) {
+              // distinguish a 2:1 violation (deeper leaves behind the face) from a hole
+              bool deeper = false;
+              for (int d = 2; d + l <= FFV_MAX_LEVEL && !deeper; d++) {
+                uint32_t fg[3];
+                for (int b = 0; b < 3; b++)
+                  fg[b] = (uint32_t)((g[b] << d) + (b == a ? (fr.side_dir > 0 ? 0 : (1 << d) - 1) : 0));
+                deeper = where.get(cell_key(l + d, fg[0], fg[1], fg[2])) >= 0;
+              }
+              bool coarser = false;
+              for (int d = 2; l - d >= 1 && !coarser; d++)
+                coarser = where.get(cell_key(l - d, (uint32_t)(g[0] >> d), (uint32_t)(g[1] >> d),
+                                             (uint32_t)(g[2] >> d))) >= 0;
+              crc[t] = (deeper || coarser) ? FFV_ERR_BALANCE : FFV_ERR_TABLE;
+              return;
+            }
+            kind = FFV_FK_FINER;
+            slot = (int32_t)(sub.size() / 4);  // shifted by the chunk's offset below
+            sub.insert(sub.end(), ids, ids + 4);
           }
-          kind = FFV_FK_FINER;
-          slot = (int32_t)(sub.size() / 4);
-          sub.insert(sub.end(), ids, ids + 4);
         }
+        info |= kind << (4 * f);
+        m->nbr[6 * c + f] = slot;
       }
-      info |= kind << (4 * f);
-      m->nbr[6 * c + f] = slot;
+      m->info[c] = info;
     }
-    m->info[c] = info;
+  };
+  {
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nthreads; t++) pool.emplace_back(work, t);
+    work(0);
+    for (auto &th : pool) th.join();
   }
+  int rc = FFV_OK;
+  for (int t = 0; t < nthreads && rc == FFV_OK; t++) rc = crc[t];
   if (rc != FFV_OK) {
     ffv_mesh_free(m);
     return rc;
+  }
+  std::vector<int32_t> sub;
+  {
+    size_t total = 0;
+    for (auto &v : csub) total += v.size();
+    sub.reserve(total);
+    for (int t = 0; t < nthreads; t++) {
+      const int32_t off = (int32_t)(sub.size() / 4);
+      if (off) {
+        const int64_t c0 = t * chunk, c1 = std::min<int64_t>(nleaves, c0 + chunk);
+        for (int64_t c = c0; c < c1; c++)
+          for (int f = 0; f < 6; f++)
+            if (ffv_face_kind(m->info[c], f) == FFV_FK_FINER) m->nbr[6 * c + f] += off;
+      }
+      sub.insert(sub.end(), csub[t].begin(), csub[t].end());
+    }
   }
   m->nsub = (int32_t)(sub.size() / 4);
   m->sub = (int32_t *)malloc(sizeof(int32_t) * (sub.size() ? sub.size() : 4));
@@ -323,6 +436,23 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
   if (!sub.empty()) memcpy(m->sub, sub.data(), sizeof(int32_t) * sub.size());
   *out = m;
   return FFV_OK;
+}
+
+int64_t ffv_sibling_group(const ffv_mesh *m, int64_t c) {
+  const int l = ffv_info_level(m->info[c]);
+  if (l <= 1) return -1;
+  const int32_t *x = m->cell_ijk + 3 * c, *t = m->tree_ijk + 3 * c;
+  const int64_t k = ((x[0] & 1) << 1) | (x[1] & 1) | ((x[2] & 1) << 2);
+  const int64_t s = c - k;
+  if (s < 0 || s + 8 > m->n) return -1;
+  for (int64_t q = 0; q < 8; q++) {
+    const int32_t *y = m->cell_ijk + 3 * (s + q), *u = m->tree_ijk + 3 * (s + q);
+    if (ffv_info_level(m->info[s + q]) != l || u[0] != t[0] || u[1] != t[1] || u[2] != t[2] ||
+        (y[0] >> 1) != (x[0] >> 1) || (y[1] >> 1) != (x[1] >> 1) || (y[2] >> 1) != (x[2] >> 1) ||
+        (((y[0] & 1) << 1) | (y[1] & 1) | ((y[2] & 1) << 2)) != q)
+      return -1;
+  }
+  return s;
 }
 
 extern "C" int64_t ffv_mesh_ncells(const ffv_mesh *m) { return m ? m->n : 0; }
