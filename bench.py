@@ -1,32 +1,41 @@
 #!/usr/bin/env python3
 """Throughput benchmark of the explicit FV step (cell-updates per second).
 
-Default workload (--workload config2): the plain FP64 form on the two-phase gas-bubble
-collapse in liquid -- liquid stiffened gas (gamma 4.4, p_inf 6e8, rho 1000, p 5e6), gas
-sphere (gamma 1.4, rho 1, p 1e5) of radius 0.1 with a tanh interface over two finest cells
-and seeded radius harmonics l <= 8 (relative amplitude 1e-3), 2^3 trees refined from level
-5 to level 8 around the interface (2.30 M cells, 2:1 balanced), transmissive sides, model
-5 (six-equation, 2 materials, NEQ 18), MUSCL-HLLC with face-state relaxation, PRELAX 3,
-RK_STEPS 2, FP64.  dt is CFL 0.01 on the liquid sound speed at the finest cell: the
-reference's model-5 scheme stops with NaN wave speeds on this problem at larger steps (its
-own C code, reproduced bit for bit by the oracle); work per step does not depend on dt.
-`--workload config1` is the 32^3 Sod problem of model 0.
+Default workload (--workload config3): gas-bubble collapse near a hyperelastic wall -- the
+half-space z < 0.2 a solid (rho 2700, stiffened-gas gamma 3.5, p_inf 3.2e10, shear modulus
+2.6e10), above it liquid (gamma 4.4, p_inf 6e8, rho 1000, p 5e6) around a gas sphere (gamma
+1.4, rho 1, p 1e5) of radius 0.1 at 1.5 radii above the wall with a tanh interface over two
+finest cells; 2^3 trees refined from level 4 to level 9 around the wall and the bubble
+(10.1 M cells), transmissive sides; model 5 with 3 materials (NEQ 21), MUSCL-HLLC with
+face-state relaxation, ghost-fluid coupling at the solid (AVF_LIM 0.5), PRELAX 3, RK_STEPS 2.
+dt is CFL 0.01 on the solid's sound speed at the finest cell: the reference's model-5 scheme
+goes non-finite on this problem within 15-20 steps at CFL 0.03 (its own C code, reproduced
+bit for bit by the oracle).  Before timing, the reference's meshadaptation with the
+configuration's criteria (relative density jump, interface layers) adapts the mesh, and
+both timed loops start from that mesh and state.
 
 One benchmark step is one time step (all RK stages) over the whole mesh; one cell-update
 is one cell advanced one time step.
 
-  value      graph-launched steps, state resident in HBM, CUDA events on the solver's
-             stream around every step; config2's state (331 MB) exceeds L2, config1's is
-             flushed from L2 (256 MiB write) between steps
-  e2e        the same through the public API with host buffers: every step uploads the
-             state from pinned host memory, runs the step and downloads the state
+  value      the metric's form: the FP32-flux form with learned AMR over `steps` steps of
+             the time loop (network every step, the plain criterion as judge every 8 steps,
+             regrids when it finds cells to refine), CUDA events on the solver's stream
+             around the loop (judges and regrids included); state resident in HBM
+  plain_fp64_amr  the comparator: plain FP64 with the reference's AMR (meshadaptation
+             every 8 steps) over the same steps
+  plain_fp64_form  plain FP64 steps alone (graph-launched, events around every step)
+  e2e        the learned loop through the public API with host buffers: every step
+             uploads the state from pinned host memory and downloads it after
   roofline   the dominant kernel's algorithmic bytes per launch over its mean duration,
              per-kernel CUDA events on the solver's stream (ffv_profile_stage)
   cpu_baseline  the oracle's C restatement of the reference algorithm, one core, on a
              bounded sample (same physics, smaller mesh)
 
-`--impl reference` times the reference algorithm on the host cores instead (the C
-restatement in oracle/, one process per core, each on the same bounded sample).
+`--workload config2` is the two-phase bubble without the wall (2.30 M cells, plain FP64
+headline), `config1` the 32^3 Sod problem of model 0; `config2m` / `config3m` are the
+medium sizes used for profiler captures.  `--impl reference` times the reference algorithm
+on the host cores instead (the C restatement in oracle/, one process per core, each on the
+same bounded sample).
 """
 from __future__ import annotations
 
@@ -119,7 +128,74 @@ def wl_config2m(small: bool = False):
     return out
 
 
-WORKLOADS = {"config2": wl_config2, "config1": wl_config1, "config2m": wl_config2m}
+C_SOLID = float(np.sqrt(3.5 * (5e6 + 3.2e10) / 2700.0))
+
+
+def _wall_solver_kwargs(p):
+    return dict(model=5, order=2, rk_steps=2, gamma=p["gamma"], pinf=p["pinf"], mu=p["mu"],
+                amin=p["amin"], avf_lim=p["avf_lim"], prelax=3)
+
+
+def wl_config3(small: bool = False, medium: bool = False):
+    """Bubble collapse near a hyperelastic wall, 3 materials (NEQ 21), levels 4-9."""
+    from forestfv_public_gb300 import workloads as W
+    if small:  # CPU sample: same physics, levels 4..5
+        lmax, band = 5, 2.0
+    elif medium:  # profiler captures: levels 4..7, 0.41 M cells
+        lmax, band = 7, 4.0
+    else:
+        lmax, band = 9, 6.5
+    mesh, S0, p = W.bubble_wall_config3(lmax=lmax, band_cells=band)
+    hmin = 0.5 / (1 << (lmax - 1))
+    dt = 0.01 * hmin / C_SOLID
+    neq = S0.shape[0]
+    size = f"levels 4-{lmax}"
+    state_mb = 8 * neq * mesh.n / 1e6
+    cfg = {"workload": f"config3 bubble collapse near a hyperelastic wall, model 5 (3 materials), "
+                       f"{size} AMR, plain FP64, MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
+           "cells": int(mesh.n), "levels": sorted(int(x) for x in np.unique(mesh.level)),
+           "neq": neq, "dt": float(dt), "cfl": 0.01, "cfl_speed": "solid sound speed, finest cell",
+           "parallelism": "single GPU",
+           "l2": f"state {state_mb:.0f} MB > L2 (129 MB): no flush needed"}
+    cfg["amr"] = {"tags": list(wall_tags(lmax)), "every": AMR_EVERY, "horizon": AMR_HORIZON,
+                  "threshold": AMR_THRESHOLD}
+    return mesh, S0, dt, cfg, _wall_solver_kwargs(p), m5_alg_bytes(neq, 3), False
+
+
+AMR_EVERY, AMR_HORIZON, AMR_THRESHOLD = 8, 16, 0.3
+WALL_LRS = 16
+
+
+def wall_tags(lmax: int) -> tuple:
+    """Refinement criteria of the wall configuration in the reference's input order:
+    uniform level 4, the relative density jump 0.1 and WALL_LRS interface layers, both to
+    the finest level."""
+    return (1, 4, 0, 0, 0.0, 1, lmax, 0.1, 0, 0, 0.0, 1, lmax, WALL_LRS, 0, 0, 0)
+
+
+def m5_alg_bytes(neq: int, nmat: int) -> dict:
+    """Algorithmic bytes per cell of each model-5 kernel (compulsory traffic, neighbour
+    re-reads excluded).  FP32 form: the FP32 shadow state (4 neq), the 2 N critical slots in
+    FP64, face records of neq + N + 1 FP32 values."""
+    d = 8 * neq
+    rec = 4 * (neq + nmat + 1)
+    return {"m5_recon_face": d + 28 + 6 * d,
+            "m5_face_flux": 6 * d + d + 28 + 6 * d + 6 * 3 * 8 + 6 * 8,
+            "m5_cell_update": d + 6 * d + 6 * 3 * 8 + d + 28 + d + d + 1,
+            "m5_relax_cell": d + d + 1,
+            "m5f_recon_face": 4 * neq + 8 * 2 * nmat + 28 + 6 * rec,
+            "m5f_face_flux": 6 * rec + 8 * 2 * nmat + 28 + 6 * 4 * neq + 6 * 3 * 4 + 6 * 8,
+            "m5f_cell_update": d + 6 * 4 * neq + 6 * 3 * 4 + d + 28 + d + d + 1,
+            "m5f_relax_cell": d + d + 1}
+
+
+def wl_config3m(small: bool = False):
+    """config3 physics on a 0.41 M-cell mesh (levels 4-7): the size profiler captures use."""
+    return wl_config3(small=small, medium=not small)
+
+
+WORKLOADS = {"config2": wl_config2, "config1": wl_config1, "config2m": wl_config2m,
+             "config3": wl_config3, "config3m": wl_config3m}
 
 
 # ------------------------------------------------------------------------------ helpers
@@ -184,15 +260,17 @@ def peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def ncu_summary(kernel: str, cells: int):
-    """(DRAM bytes per launch, FP64-pipe % busy) of a kernel from the committed ncu summary
-    (bytes per cell x cells); None where the kernel has no capture."""
+def ncu_summary(kernel: str, cells: int, workload: str):
+    """(DRAM bytes per launch, FP64-pipe % busy) of a kernel on a workload family (config2
+    for config2 and config2m, ...) from the committed ncu summary (bytes per cell x cells);
+    None where the kernel has no capture."""
+    fam = workload[:-1] if workload.endswith("m") else workload
     p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     try:
         for ln in open(p):
             t = ln.split()
-            if len(t) >= 2 and not ln.startswith("#") and t[0] == kernel:
-                return float(t[1]) * cells, (float(t[2]) if len(t) > 2 else None)
+            if len(t) >= 3 and not ln.startswith("#") and t[0] == kernel and t[1] == fam:
+                return float(t[2]) * cells, (float(t[3]) if len(t) > 3 else None)
     except OSError:
         pass
     return None, None
@@ -329,6 +407,99 @@ def measure_fp32_form(mesh, S0, dt, kw, args, dev, fp64_solver) -> dict:
                     "differences, so the FP32 form is judged against that floor"}
 
 
+def train_wall_indicator(kw: dict, dev, amr_cfg: dict, seed: int = 20261203):
+    """The indicator of the wall configuration, trained on the GPU on seeded runs of its
+    medium size (levels 4-7) with standoffs U(1.0, 2.5) and bubble radii U(0.05, 0.15):
+    snapshots of (features, "the criterion asks for a finer level within `horizon`
+    steps"), a criterion-driven regrid between snapshots, then AdamW (lr 1e-3, batch
+    8192).  Returns the indicator and a summary."""
+    import torch
+
+    from forestfv_public_gb300 import Solver
+    from forestfv_public_gb300 import workloads as W
+    from forestfv_public_gb300.amr import AdaptiveRun
+    from forestfv_public_gb300.indicator import Indicator, collect_window, field_norm
+    t0 = time.perf_counter()
+    rng = np.random.default_rng(seed)
+    ind = Indicator(device=dev.index, seed=seed)
+    tags7 = wall_tags(7)
+    dt7 = 0.01 * (0.5 / (1 << 6)) / C_SOLID
+    Xs, ys, runs = [], [], 0
+    for k in range(3):
+        standoff, radius = rng.uniform(1.0, 2.5), rng.uniform(0.05, 0.15)
+        mesh, S0, _ = W.bubble_wall_config3(lmax=7, band_cells=4.0, radius=radius,
+                                            standoff=standoff)
+        s = Solver(device=dev.index, precision=1, **kw)
+        s.set_mesh(mesh)
+        s.upload_state(S0)
+        amr = AdaptiveRun(s, tags7)
+        amr.meshadaptation()
+        if k == 0:
+            mean, std = field_norm([ind.fields(s).cpu().numpy()])
+            ind.set_norm(mean, np.maximum(std, np.array([0.05, 0.05, 0.01, 0.01, 1.0],
+                                                         np.float32)))
+        for _ in range(3):
+            X, y = collect_window(s, ind, tags7, dt7, amr_cfg["horizon"])
+            Xs.append(X)
+            ys.append(y)
+            amr.meshadaptation()
+        s.close()
+        runs += 1
+    X, y = torch.cat(Xs), torch.cat(ys)
+    losses = ind.train(X, y, steps=800, batch=8192, lr=1e-3, wd=1e-4, seed=seed)
+    return ind, {"runs": runs, "pairs": int(X.shape[0]), "positive_fraction": float(y.mean()),
+                 "loss_first": float(losses[:10].mean()), "loss_last": float(losses[-50:].mean()),
+                 "train_steps": 800, "seconds": time.perf_counter() - t0}
+
+
+def timed_amr_loop(solver, amr, dt, steps, warmup, stream, host=False):
+    """Run `warmup` untimed and `steps` timed steps of an AdaptiveRun; CUDA events on the
+    solver's stream bracket the timed steps (the host work of judges and regrids happens
+    between them, so the events see it).  With host=True every step uploads the state from
+    pinned host memory first and downloads it after (the end-to-end form).  Returns
+    (seconds, cell-updates, h2d bytes, d2h bytes)."""
+    import torch
+    amr.run(dt, warmup)
+    cu0 = amr.stats.cell_updates
+    buf = None
+    h2d = d2h = 0
+    if host:
+        buf = torch.empty((solver.neq, solver.mesh.n), dtype=torch.float64, pin_memory=True).numpy()
+        buf[:] = solver.download_state()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+    for _ in range(steps):
+        if host:
+            if buf.shape[1] != solver.mesh.n:
+                buf = torch.empty((solver.neq, solver.mesh.n), dtype=torch.float64,
+                                  pin_memory=True).numpy()
+                buf[:] = solver.download_state()
+            solver.upload_state(buf)
+            h2d += buf.nbytes
+        amr.run(dt, 1)
+        if host:
+            if buf.shape[1] != solver.mesh.n:
+                buf = torch.empty((solver.neq, solver.mesh.n), dtype=torch.float64,
+                                  pin_memory=True).numpy()
+            buf[:] = solver.download_state()
+            d2h += buf.nbytes
+    with torch.cuda.stream(stream):
+        e1.record(stream)
+    solver.sync()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3, amr.stats.cell_updates - cu0, h2d, d2h
+
+
+def amr_launches(solver, st, judge_launches: int) -> int:
+    """Kernel launches of an AdaptiveRun's steps, judges and inferences (regrids not
+    counted): launches per step x steps, judge_launches per judge, 3 per inference
+    (fields, gather, forward)."""
+    infer = st.steps if st.t_infer > 0 else 0
+    return solver.launches_per_step() * st.steps + judge_launches * st.judged + 3 * infer
+
+
 def run_ours(args) -> None:
     import torch
 
@@ -344,9 +515,21 @@ def run_ours(args) -> None:
     torch.cuda.set_device(dev)
 
     mesh, S0, dt, cfg, kw, alg_bytes, flush_l2 = WORKLOADS[args.workload]()
+    amr_cfg = cfg.get("amr") if not args.no_amr else None
     solver = Solver(device=local, **kw)
     solver.set_mesh(mesh)
     solver.upload_state(S0)
+    if amr_cfg is not None:
+        # the timed loops start from the criterion's own mesh (the reference's meshadaptation
+        # on the initial state), untimed
+        from forestfv_public_gb300.amr import AdaptiveRun
+        t0 = time.perf_counter()
+        rounds = AdaptiveRun(solver, amr_cfg["tags"]).meshadaptation()
+        mesh = solver.mesh
+        S0 = solver.download_state()
+        cfg["initial_adaptation"] = {"rounds": rounds, "seconds": time.perf_counter() - t0,
+                                     "cells": int(mesh.n),
+                                     "levels": sorted(int(x) for x in np.unique(mesh.level))}
     neq = solver.neq
     stream = torch.cuda.ExternalStream(solver.stream_handle(), device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev) if flush_l2 else None
@@ -369,42 +552,44 @@ def run_ours(args) -> None:
         ev[k][1].record(stream)
     solver.sync()
     torch.cuda.synchronize(dev)
-    clock_info = clocks.stop()
     t_ms = sum(a.elapsed_time(b) for a, b in ev)
     if world > 1:
         t = torch.tensor([t_ms], device=dev, dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         t_ms = float(t.item())
-    value = world * mesh.n * args.steps / (t_ms / 1e3)
+    value_fp64 = world * mesh.n * args.steps / (t_ms / 1e3)
 
-    # per-kernel durations for the roofline (same stages, events around every kernel)
-    per_kernel = {}
-    nprof = max(3, min(args.steps, 10))
-    for _ in range(nprof):
-        for irk in (1, 2):
-            if flush is not None:
-                with torch.cuda.stream(stream):
-                    flush.zero_()
-            for name, ms in solver.profile_stage(irk, dt).items():
-                per_kernel.setdefault(name, []).append(ms)
-    mean_ms = {k: sum(v) / len(v) for k, v in per_kernel.items()}
-    dom = max(mean_ms, key=mean_ms.get)
-    peak, peak_kind = peak_hbm()
-    alg = alg_bytes.get(dom, 0) * mesh.n
-    achieved = alg / (mean_ms[dom] / 1e3) / 1e9
-    step_ms = sum(mean_ms.values())
-    traffic, fp64_pct = ncu_summary(dom, mesh.n)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    def kernel_times(s, nprof):
+        per = {}
+        for _ in range(nprof):
+            for irk in (1, 2):
+                if flush is not None:
+                    with torch.cuda.stream(stream):
+                        flush.zero_()
+                for name, ms in s.profile_stage(irk, dt).items():
+                    per.setdefault(name, []).append(ms)
+        return {k: sum(v) / len(v) for k, v in per.items()}
+
+    def roofline_of(mean_ms, n, note):
+        dom = max(mean_ms, key=mean_ms.get)
+        peak, peak_kind = peak_hbm()
+        alg = alg_bytes.get(dom, 0) * n
+        achieved = alg / (mean_ms[dom] / 1e3) / 1e9
+        step_ms = sum(mean_ms.values())
+        traffic, pipe_pct = ncu_summary(dom, n, args.workload)
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "kernel": dom,
-                "fp64_pipe_busy_pct_ncu": fp64_pct,
+                "fp64_pipe_busy_pct_ncu": pipe_pct,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst)",
                 "kernel_mean_ms_per_stage": mean_ms,
                 "kernel_share": {k: v / step_ms for k, v in mean_ms.items()},
-                "alg_bytes_per_launch": alg,
-                "note": "the FP64 kernels are FP64-pipe bound (GB300 FP64 = 1/64 FP32), "
-                        "see profiles/"}
+                "alg_bytes_per_launch": alg, "note": note}
 
-    # end to end through the public API with pinned host buffers
+    roof64 = roofline_of(kernel_times(solver, max(3, min(args.steps, 10))), mesh.n,
+                         "the FP64 kernels are FP64-pipe bound (GB300 FP64 = 1/64 FP32), "
+                         "see profiles/")
+
+    # end to end through the public API with pinned host buffers (plain FP64 form)
     host = torch.empty((neq, mesh.n), dtype=torch.float64, pin_memory=True).numpy()
     host[:] = S0
     torch.cuda.synchronize(dev)
@@ -415,9 +600,9 @@ def run_ours(args) -> None:
         solver.step(dt, 1)
         host[:] = solver.download_state()
     e2e_s = time.perf_counter() - t0
-    e2e = {"value": world * mesh.n * e2e_steps / e2e_s, "unit": UNIT,
-           "h2d_bytes_per_step": neq * 8 * mesh.n, "d2h_bytes_per_step": neq * 8 * mesh.n,
-           "steps": e2e_steps}
+    e2e64 = {"value": world * mesh.n * e2e_steps / e2e_s, "unit": UNIT,
+             "h2d_bytes_per_step": neq * 8 * mesh.n, "d2h_bytes_per_step": neq * 8 * mesh.n,
+             "steps": e2e_steps}
 
     if rank == 0:
         cpu = None
@@ -429,21 +614,102 @@ def run_ours(args) -> None:
         fp32 = None
         if world == 1 and kw.get("model", 0) == 5 and not args.no_fp32_form:
             fp32 = measure_fp32_form(mesh, S0, dt, kw, args, dev, solver)
-            fp32["speedup_vs_fp64"] = fp32["value"] / value
+            fp32["speedup_vs_fp64"] = fp32["value"] / value_fp64
+        fp64_line = {"value": value_fp64, "unit": UNIT, "ms_per_step": t_ms / args.steps,
+                     "e2e": e2e64, "roofline": roof64,
+                     "gpu_launches": solver.launches_per_step() * args.steps}
         line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": cfg, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
-            "clocks": clock_info,
-            "gpu_launches": solver.launches_per_step() * args.steps,
+            "metric": METRIC, "value": value_fp64, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": cfg, "e2e": e2e64, "roofline": roof64,
+            "cpu_baseline": cpu, "gpu_launches": fp64_line["gpu_launches"],
         }
+        if amr_cfg is not None and world == 1:
+            line.update(measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes,
+                                    roofline_of, kernel_times, stream))
+            line["plain_fp64_form"] = fp64_line
         if fp32 is not None:
             line["fp32_flux_form"] = fp32
+        line["clocks"] = clocks.stop()
         print(json.dumps(line), flush=True)
+    else:
+        clocks.stop()
     solver.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, kernel_times,
+                stream64) -> dict:
+    """The metric's two forms over the time loop with mesh adaptation, both from the
+    criterion-adapted mesh and state: plain FP64 with plain AMR (the reference's loop,
+    meshadaptation every `every` steps) and the FP32-flux form with learned AMR (network
+    every step, the criterion as judge every `every` steps, regrids only when it finds
+    cells to refine or after three skips).  Returns the keys of the headline line."""
+    import torch
+
+    from forestfv_public_gb300 import Solver
+    from forestfv_public_gb300.amr import AdaptiveRun
+    from forestfv_public_gb300.fields import error_report_meshes
+    ind, train = train_wall_indicator(kw, dev, amr_cfg)
+    tags = tuple(amr_cfg["tags"])
+    every, thr = amr_cfg["every"], amr_cfg["threshold"]
+    si_max = tags[13] if tags[11] == 1 else 0
+    judge_launches = (si_max + 1) if tags[11] == 1 else 2
+
+    def fresh(precision):
+        s = Solver(device=dev.index, precision=precision, **kw)
+        s.set_mesh(mesh)
+        s.upload_state(S0)
+        return s
+
+    # plain FP64 + plain AMR
+    sp = fresh(0)
+    plain = AdaptiveRun(sp, tags, every=every)
+    st_p = torch.cuda.ExternalStream(sp.stream_handle(), device=dev)
+    sec_p, cu_p, _, _ = timed_amr_loop(sp, plain, dt, args.steps, args.warmup, st_p)
+    # FP32 flux + learned AMR
+    sl = fresh(1)
+    learned = AdaptiveRun(sl, tags, every=every, indicator=ind, threshold=thr)
+    st_l = torch.cuda.ExternalStream(sl.stream_handle(), device=dev)
+    sec_l, cu_l, _, _ = timed_amr_loop(sl, learned, dt, args.steps, args.warmup, st_l)
+    mu = kw.get("mu")
+    solid = 0 if mu is not None and mu[0] != 0.0 else None
+    err = error_report_meshes(sl.mesh, sl.download_state(), sp.mesh, sp.download_state(),
+                              kw["gamma"], kw["pinf"], mu, kw["amin"], solid)
+    roof32 = roofline_of(kernel_times(sl, 3), sl.mesh.n,
+                         "FP32-flux form; its face kernel mixes FP32 arithmetic with the FP64 "
+                         "pressure recovery of the critical slots")
+    # the learned form end to end: state uploaded from and downloaded to pinned host memory
+    # around every step of the same loop
+    se = fresh(1)
+    e2e_run = AdaptiveRun(se, tags, every=every, indicator=ind, threshold=thr)
+    st_e = torch.cuda.ExternalStream(se.stream_handle(), device=dev)
+    sec_e, cu_e, h2d, d2h = timed_amr_loop(se, e2e_run, dt, args.steps, args.warmup, st_e,
+                                           host=True)
+    value = cu_l / sec_l
+    plain_value = cu_p / sec_p
+    out = {
+        "value": value, "ms_per_step": 1e3 * sec_l / args.steps,
+        "dtype": "f32 flux, f64 state and residuals",
+        "form": "FP32-flux + learned AMR",
+        "e2e": {"value": cu_e / sec_e, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps, "steps": args.steps},
+        "roofline": roof32,
+        "gpu_launches": amr_launches(sl, learned.stats, judge_launches),
+        "plain_fp64_amr": {"value": plain_value, "unit": UNIT,
+                           "ms_per_step": 1e3 * sec_p / args.steps,
+                           "amr": plain.stats.as_dict()},
+        "learned_amr": {"amr": learned.stats.as_dict(), "indicator_training": train,
+                        "every": every, "horizon": amr_cfg["horizon"], "threshold": thr,
+                        "error_vs_plain_fp64_amr": err,
+                        "speedup_vs_plain_fp64_amr": value / plain_value},
+    }
+    for s in (sp, sl, se):
+        s.close()
+    ind.close()
+    return out
 
 
 def main() -> None:
@@ -452,8 +718,10 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
-    ap.add_argument("--workload", default="config2", choices=tuple(WORKLOADS))
+    ap.add_argument("--workload", default="config3", choices=tuple(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-amr", action="store_true",
+                    help="skip the time loops with mesh adaptation (headline = plain FP64)")
     ap.add_argument("--no-fp32-form", action="store_true",
                     help="skip the FP32-flux form's throughput and error report")
     args = ap.parse_args()

@@ -77,7 +77,7 @@ EXPORTS = (
     "ffv_destroy", "ffv_set_mesh", "ffv_upload_state", "ffv_download_state", "ffv_stage",
     "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
     "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
-    "ffv_tags", "ffv_tags_smooth", "ffv_adapt", "ffv_mesh_leaves",
+    "ffv_tags", "ffv_tags_raw", "ffv_tags_missed", "ffv_tags_smooth", "ffv_adapt", "ffv_mesh_leaves",
     "ffv_mlp_create", "ffv_mlp_destroy", "ffv_mlp_get_params", "ffv_mlp_set_params",
     "ffv_mlp_set_norm", "ffv_mlp_fields", "ffv_mlp_features", "ffv_mlp_forward",
     "ffv_mlp_predict", "ffv_mlp_grad", "ffv_mlp_train",
@@ -117,6 +117,8 @@ def lib() -> ctypes.CDLL:
     L.ffv_stage_kernel_name.restype = ctypes.c_char_p
     L.ffv_launches_per_step.argtypes = [vp, ctypes.POINTER(i32)]
     L.ffv_tags.argtypes = [vp, vp, ctypes.POINTER(TagParams), vp, vp, vp]
+    L.ffv_tags_raw.argtypes = [vp, vp, ctypes.POINTER(TagParams), vp, vp]
+    L.ffv_tags_missed.argtypes = [vp, vp, ctypes.POINTER(TagParams), ctypes.POINTER(i64)]
     L.ffv_tags_smooth.argtypes = [vp, i32, vp]
     L.ffv_adapt.argtypes = [vp, vp, vp, ctypes.POINTER(vp)]
     L.ffv_mesh_leaves.argtypes = [vp, vp, vp, vp]

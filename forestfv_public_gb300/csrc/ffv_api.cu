@@ -532,9 +532,13 @@ int ffv_stream(ffv_ctx *c, void **stream) {
   return FFV_OK;
 }
 
-int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split,
-             int32_t *split_raw, int32_t *si) {
-  if (!c || !m || !p || !split) return FFV_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+// the device half of ffv_tags: SI layers and the raw target level of every leaf into
+// c->d_split; *level_max receives the reference's LEVEL
+int tags_device(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *level_max) {
   if (!c->have_state) return FFV_ERR_STATE;
   if (m->n != c->n) return FFV_ERR_ARG;
   if (p->inter0 == 0 && p->inter1 == 1) return FFV_ERR_ARG;  // m5_input.c:52 exits there
@@ -551,9 +555,10 @@ int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *sp
   if (p->inter0 == 1 && p->inter1 == 1) t.si_max = t.lrs0 + t.lrs1;
   if (p->inter0 == 1 && p->inter1 == 0) t.si_max = t.lrs0;
   // inputset.c:106, m5_input.c:53
-  int32_t level_max = p->lvl_uniform;
+  int32_t lmax = p->lvl_uniform;
   for (int32_t l : {p->lvl_prs, p->lvl_rho, p->lvl_vel, p->lvl_inter0, p->lvl_inter1})
-    level_max = level_max > l ? level_max : l;
+    lmax = lmax > l ? lmax : l;
+  *level_max = lmax;
   CK(cudaSetDevice(c->device));
   const int64_t n = c->n;
   if (!c->d_split) {
@@ -574,12 +579,67 @@ int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *sp
     CK(cudaMemsetAsync(c->d_SI, 0, sizeof(int32_t) * 2 * n, c->stream));
   }
   CK(cudaGetLastError());
+  return FFV_OK;
+}
+
+// leaves whose target level is above their level (warp sums, one atomic per warp)
+__global__ void count_finer(int64_t n, const uint32_t *__restrict__ info,
+                            const int32_t *__restrict__ split, unsigned long long *count) {
+  unsigned long long k = 0;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    k += split[c] > (int32_t)ffv_info_level(info[c]) ? 1ull : 0ull;
+  for (int o = 16; o > 0; o >>= 1) k += __shfl_down_sync(0xffffffffu, k, o);
+  if ((threadIdx.x & 31) == 0 && k) atomicAdd(count, k);
+}
+
+}  // namespace
+
+extern "C" {
+
+int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split,
+             int32_t *split_raw, int32_t *si) {
+  if (!c || !m || !p || !split) return FFV_ERR_ARG;
+  int32_t level_max;
+  int rc = tags_device(c, m, p, &level_max);
+  if (rc != FFV_OK) return rc;
+  const int64_t n = c->n;
   CK(cudaMemcpyAsync(split, c->d_split, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
   if (si)
     CK(cudaMemcpyAsync(si, c->d_SI, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   if (split_raw) memcpy(split_raw, split, sizeof(int32_t) * n);
   return ffv_tags_smooth(m, level_max, split);
+}
+
+int ffv_tags_raw(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split_raw,
+                 int32_t *si) {
+  if (!c || !m || !p || !split_raw) return FFV_ERR_ARG;
+  int32_t level_max;
+  int rc = tags_device(c, m, p, &level_max);
+  if (rc != FFV_OK) return rc;
+  const int64_t n = c->n;
+  CK(cudaMemcpyAsync(split_raw, c->d_split, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                     c->stream));
+  if (si)
+    CK(cudaMemcpyAsync(si, c->d_SI, sizeof(int32_t) * 2 * n, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return FFV_OK;
+}
+
+int ffv_tags_missed(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int64_t *missed) {
+  if (!c || !m || !p || !missed) return FFV_ERR_ARG;
+  int32_t level_max;
+  int rc = tags_device(c, m, p, &level_max);
+  if (rc != FFV_OK) return rc;
+  CK(cudaMemsetAsync(c->d_red, 0, sizeof(unsigned long long), c->stream));
+  count_finer<<<152 * 4, 256, 0, c->stream>>>(c->n, c->d_info, c->d_split, c->d_red);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->h_red, c->d_red, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  *missed = (int64_t)*c->h_red;
+  return FFV_OK;
 }
 
 int ffv_launches_per_step(const ffv_ctx *c, int32_t *n) {

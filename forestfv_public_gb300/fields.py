@@ -78,3 +78,61 @@ def error_report(S_test: np.ndarray, S_ref: np.ndarray, gamma, pinf, mu, amin: f
             out["peak_wall_stress"] = {"test": pa, "ref": pb,
                                        "rel_err": abs(pa - pb) / max(abs(pb), 1e-300)}
     return out
+
+
+def to_uniform(mesh, F: np.ndarray, level: int) -> np.ndarray:
+    """Cell values F [..., n] of an adaptive mesh painted onto the uniform grid of `level`
+    (every leaf at or below that level covers 8^(level - l) fine cells): [..., X, Y, Z].
+    Fields of two runs on different meshes are compared on this grid."""
+    T = np.asarray(mesh.ntrees)
+    e = 1 << (level - 1)
+    out = np.zeros(F.shape[:-1] + tuple(int(t) * e for t in T), dtype=F.dtype)
+    for l in np.unique(mesh.level):
+        idx = np.flatnonzero(mesh.level == l)
+        r = 1 << (level - int(l))
+        if r < 1:
+            raise ValueError("mesh finer than the target grid")
+        g = (mesh.tree_ijk[idx].astype(np.int64) * (1 << (int(l) - 1)) + mesh.cell_ijk[idx]) * r
+        o = np.arange(r)
+        ox, oy, oz = np.meshgrid(o, o, o, indexing="ij")
+        X = (g[:, 0, None] + ox.ravel()[None]).ravel()
+        Y = (g[:, 1, None] + oy.ravel()[None]).ravel()
+        Z = (g[:, 2, None] + oz.ravel()[None]).ravel()
+        vals = np.repeat(F[..., idx], r ** 3, axis=-1)
+        out[..., X, Y, Z] = vals
+    return out
+
+
+def same_leaves(ma, mb) -> bool:
+    return (ma.n == mb.n and np.array_equal(ma.level, mb.level)
+            and np.array_equal(ma.tree_ijk, mb.tree_ijk) and np.array_equal(ma.cell_ijk, mb.cell_ijk))
+
+
+def error_report_meshes(ma, Sa, mb, Sb, gamma, pinf, mu, amin: float = 1e-6,
+                        solid: int | None = None) -> dict:
+    """error_report of run a against run b when their meshes may differ: cell by cell on
+    identical leaves, otherwise on the uniform grid of the finest level of either mesh
+    (each leaf's density, pressure, volume fraction and von Mises stress painted over the
+    fine cells it covers; float32)."""
+    if same_leaves(ma, mb):
+        out = error_report(Sa, Sb, gamma, pinf, mu, amin, solid)
+        out["compared_on"] = "identical leaves"
+        return out
+    lev = int(max(ma.level.max(), mb.level.max()))
+    pa = primitives(Sa, gamma, pinf, mu, amin)
+    pb = primitives(Sb, gamma, pinf, mu, amin)
+    out = {"compared_on": f"uniform grid of level {lev}"}
+    for key, fa, fb in (("rho", pa["rho"], pb["rho"]), ("p", pa["p"], pb["p"]),
+                        ("alpha", pa["alpha"][0], pb["alpha"][0])):
+        x = to_uniform(ma, fa.astype(np.float32), lev)
+        y = to_uniform(mb, fb.astype(np.float32), lev)
+        d = np.abs(x.astype(np.float64) - y)
+        out[key] = {"rel_l1": float(d.sum() / max(np.abs(y).astype(np.float64).sum(), 1e-300)),
+                    "rel_linf": float(d.max() / max(float(np.abs(y).max()), 1e-300))}
+        del x, y, d
+    if solid is not None:
+        ka, kb = pa["alpha"][solid] > 0.5, pb["alpha"][solid] > 0.5
+        if ka.any() and kb.any():
+            va, vb = float(pa["vm"][ka].max()), float(pb["vm"][kb].max())
+            out["peak_wall_stress"] = {"test": va, "ref": vb, "rel_err": abs(va - vb) / max(abs(vb), 1e-300)}
+    return out

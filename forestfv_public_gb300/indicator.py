@@ -136,6 +136,21 @@ def collect(solver, indicator: Indicator, tag_params, dt: float, snapshots: int,
     return X, y, tags_now, tags_future
 
 
+def collect_window(solver, indicator: Indicator, tag_params, dt: float, horizon: int):
+    """One training snapshot for pre-refinement: the feature rows of the current state and
+    the label "the plain criterion asks for a finer level than the cell has at some step
+    of the next `horizon`" (raw criterion levels, ffv_tags_raw, one per step).  Advances the
+    solver `horizon` steps on its current mesh.  Returns device X [n, 144] and y [n]."""
+    import torch
+    level = solver.mesh.level
+    X = indicator.features(solver)
+    hit = np.zeros(solver.mesh.n, bool)
+    for _ in range(horizon):
+        solver.step(dt, 1)
+        hit |= solver.tags_raw(tag_params) > level
+    return X, torch.from_numpy(hit.astype(np.float32)).to(X.device)
+
+
 def coverage(flag_now: np.ndarray, flag_future: np.ndarray) -> tuple[float, int]:
     """Fraction of the cells flagged at the future step that are flagged now, and the number
     of cells flagged now."""

@@ -18,6 +18,43 @@ from . import _lib
 from .mesh import Mesh
 
 
+def level_max(params) -> int:
+    """The reference's LEVEL: the largest level any criterion names (inputset.c:106)."""
+    return max(params.lvl_uniform, params.lvl_prs, params.lvl_rho, params.lvl_vel,
+               params.lvl_inter0, params.lvl_inter1)
+
+
+def would_change(mesh: Mesh, split: np.ndarray) -> bool:
+    """Whether a refineh pass with targets `split` changes any leaf: a leaf wants a finer
+    level, or eight sibling leaves (consecutive, child indices 0..7, one parent) all want a
+    coarser one (refineh.c:10-57)."""
+    lev = mesh.level
+    if np.any(split > lev):
+        return True
+    low = split < lev
+    if not low.any():
+        return False
+    c = mesh.cell_ijk
+    kid = ((c[:, 0] & 1) << 1) | (c[:, 1] & 1) | ((c[:, 2] & 1) << 2)
+    s = np.flatnonzero(low & (kid == 0) & (lev > 1))
+    s = s[s + 7 < lev.size]
+    ok = np.ones(s.size, bool)
+    for q in range(1, 8):
+        j = s + q
+        ok &= (low[j] & (kid[j] == q) & (lev[j] == lev[s])
+               & np.all(mesh.tree_ijk[j] == mesh.tree_ijk[s], axis=1)
+               & np.all((c[j] >> 1) == (c[s] >> 1), axis=1))
+    return bool(ok.any())
+
+
+def tags_smooth(mesh: Mesh, lmax: int, split: np.ndarray) -> np.ndarray:
+    """criterionsmth (ffv_tags_smooth) on a copy of the target levels `split`."""
+    out = np.ascontiguousarray(split, dtype=np.int32).copy()
+    _lib.check(_lib.lib().ffv_tags_smooth(mesh.handle, int(lmax), out.ctypes.data),
+               "ffv_tags_smooth")
+    return out
+
+
 class Solver:
     def __init__(self, model: int = 0, order: int = 2, rk_steps: int = 2, gamma=(1.4,),
                  pinf=(0.0,), precision: int = _lib.FFV_FP64, device: int = 0, mu=None,
@@ -90,6 +127,25 @@ class Solver:
                                        si.ctypes.data if with_raw else None), "ffv_tags")
         return (split, raw, si) if with_raw else split
 
+    def tags_raw(self, params) -> np.ndarray:
+        """The criterion's target level per cell before smoothing (ffv_tags_raw)."""
+        if not isinstance(params, _lib.TagParams):
+            params = _lib.TagParams.from_tuple(params)
+        split = np.empty(self.mesh.n, np.int32)
+        _lib.check(_lib.lib().ffv_tags_raw(self._h, self.mesh.handle, ctypes.byref(params),
+                                           split.ctypes.data, None), "ffv_tags_raw")
+        return split
+
+    def tags_missed(self, params) -> int:
+        """Number of cells whose raw target level is above their level (ffv_tags_missed):
+        the plain criterion as a judge, counted on the device."""
+        if not isinstance(params, _lib.TagParams):
+            params = _lib.TagParams.from_tuple(params)
+        out = ctypes.c_int64()
+        _lib.check(_lib.lib().ffv_tags_missed(self._h, self.mesh.handle, ctypes.byref(params),
+                                              ctypes.byref(out)), "ffv_tags_missed")
+        return int(out.value)
+
     def adapt(self, split) -> Mesh:
         """One refineh pass (ffv_adapt) with target levels `split`; the solver continues on
         the returned mesh with the carried-over state."""
@@ -107,10 +163,11 @@ class Solver:
         refinement tags and one refineh pass, LEVEL the largest level the criteria name."""
         if not isinstance(params, _lib.TagParams):
             params = _lib.TagParams.from_tuple(params)
-        level = max(params.lvl_uniform, params.lvl_prs, params.lvl_rho, params.lvl_vel,
-                    params.lvl_inter0, params.lvl_inter1)
-        for _ in range(level + 1):
-            self.adapt(self.tags(params))
+        for _ in range(level_max(params) + 1):
+            split = self.tags(params)
+            if not would_change(self.mesh, split):
+                break  # every further round sees the same state and mesh
+            self.adapt(split)
         return self.mesh
 
     def cfl_dt(self, cfl: float) -> float:

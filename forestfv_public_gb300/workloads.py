@@ -111,6 +111,67 @@ def mixture_state(mat: dict, a_gas: np.ndarray) -> np.ndarray:
     return S
 
 
+WALL = dict(gamma=(3.5, 4.4, 1.4), pinf=(3.2e10, 6e8, 0.0), rho=(2700.0, 1000.0, 1.0),
+            p=(5e6, 5e6, 1e5), mu=(2.6e10, 0.0, 0.0), amin=1e-6, avf_lim=0.5)
+
+
+def bubble_wall_config3(lmin: int = 4, lmax: int = 9, band_cells: float = 6.5,
+                        radius: float = 0.1, standoff: float = 1.5, wall_z: float = 0.2):
+    """Gas bubble collapse near a solid wall (the third configuration): the half-space
+    z < wall_z is a hyperelastic solid (material 0: rho 2700, stiffened-gas gamma 3.5,
+    p_inf 3.2e10, shear modulus 2.6e10), above it liquid (material 1, as in the second
+    configuration) around a gas sphere (material 2) of radius 0.1 centred standoff radii
+    above the wall, its interface smoothed over two finest cells with tanh in volume
+    fraction; 2^3 trees, levels lmin..lmax refined around the wall plane and the bubble
+    (9.9 M cells at the default sizes).  The solid cells take the reference's m5_init_S
+    state (init_S.c:205-266: the cell's material at 1 - 2 AMIN, the others at AMIN,
+    deformation A = I; A = 0 in fluid cells).  Returns (Mesh, S [21, n], params)."""
+    c0 = np.array([0.5, 0.5, wall_z + standoff * radius])
+    hmin = 0.5 / (1 << (lmax - 1))
+
+    def target(cen, h):
+        r = np.linalg.norm(cen - c0, axis=1)
+        d = np.minimum(np.abs(r - radius), np.abs(cen[:, 2] - wall_z)) - 0.8660254 * h
+        lev = lmax - np.floor(np.maximum(d, 0.0) / (band_cells * hmin * 2.0)).astype(np.int64)
+        return np.maximum(lev, lmin)
+
+    leaves = refine_to_target((2, 2, 2), lmin, lmax, target)
+    mesh = Mesh((2, 2, 2), leaves)
+    x = mesh.centroids()
+    r = np.linalg.norm(x - c0, axis=1)
+    a_gas = 0.5 * (1.0 - np.tanh((r - radius) / (2.0 * hmin)))
+    S = wall_state(WALL, x[:, 2] < wall_z, a_gas)
+    return mesh, S, dict(WALL)
+
+
+def wall_state(mat: dict, solid: np.ndarray, a_gas: np.ndarray) -> np.ndarray:
+    """Three-material state [neq=21, n] at rest: material 0 solid, 1 liquid, 2 gas.  Solid
+    cells: the solid at 1 - 2 AMIN at its initial pressure, A = I.  Fluid cells: the solid
+    at AMIN, gas fraction a_gas (clipped to [AMIN, 1 - 2 AMIN]), the liquid the rest, at the
+    volume-fraction-weighted pressure, A = 0 (no elastic energy in either)."""
+    amin = mat["amin"]
+    N = 3
+    n = len(a_gas)
+    ag = np.where(solid, amin, np.clip(a_gas, amin, 1.0 - 2.0 * amin))
+    asol = np.where(solid, 1.0 - 2.0 * amin, amin)
+    aliq = 1.0 - asol - ag
+    alpha = (asol, aliq, ag)
+    p = np.where(solid, mat["p"][0], aliq * mat["p"][1] + ag * mat["p"][2])
+    S = np.zeros((3 * N + 12, n))
+    E = np.zeros(n)
+    for k in range(N):
+        S[k] = alpha[k] * mat["rho"][k]
+        are = alpha[k] * (p + mat["gamma"][k] * mat["pinf"][k]) / (mat["gamma"][k] - 1.0)
+        S[2 * N + 3 + k] = are
+        E += are
+    S[N + 3] = E
+    S[N + 4] = asol
+    S[N + 5] = aliq
+    for q in (0, 4, 8):
+        S[3 * N + 3 + q] = np.where(solid, 1.0, 0.0)
+    return S
+
+
 def blast_m0(mesh: Mesh, center, radius: float, p_in: float = 10.0, p_out: float = 0.1,
              rho_in: float = 1.0, rho_out: float = 0.125, gamma: float = 1.4) -> np.ndarray:
     """Model-0 spherical blast at rest: (rho_in, p_in) inside the sphere, (rho_out, p_out)

@@ -180,6 +180,15 @@ typedef struct ffv_tag_params {
  * relative jumps of the cell states, and no interface layers. */
 int ffv_tags(ffv_ctx *ctx, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split,
              int32_t *split_raw, int32_t *si);
+/* ffv_tags without the smoothing: the raw target level per leaf (and optionally SI), for
+ * callers that combine it with other targets before ffv_tags_smooth. */
+int ffv_tags_raw(ffv_ctx *ctx, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split_raw,
+                 int32_t *si);
+/* The plain criterion as a judge (no counterpart in the reference): the device part of
+ * ffv_tags (SI layers and the raw target levels) and, on the device, the number of leaves
+ * whose raw target level is above their level -- the leaves a regrid would refine.  No
+ * host smoothing, one 8-byte copy back. */
+int ffv_tags_missed(ffv_ctx *ctx, const ffv_mesh *m, const ffv_tag_params *p, int64_t *missed);
 /* criterionsmth alone, in place on split[n] (host): level_max is the reference's LEVEL,
  * the largest level any criterion names. */
 int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *split);

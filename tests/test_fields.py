@@ -56,3 +56,20 @@ def test_error_report_keys_and_zero():
     rep = error_report(S, S, BUBBLE["gamma"], BUBBLE["pinf"], BUBBLE["mu"])
     for k in ("rho", "p", "alpha"):
         assert rep[k]["rel_l1"] == 0.0 and rep[k]["rel_linf"] == 0.0
+
+
+def test_to_uniform_paints_leaves(built_lib):
+    from forestfv_public_gb300 import Mesh
+    from forestfv_public_gb300.fields import to_uniform
+    from forestfv_public_gb300.workloads import refine_to_target
+    leaves = refine_to_target((2, 2, 2), 2, 4,
+                              lambda c, h: np.where(c[:, 0] < 0.25, 4, np.where(c[:, 0] < 0.5, 3, 2)))
+    m = Mesh((2, 2, 2), leaves)
+    x = m.centroids()
+    U = to_uniform(m, x.T.copy(), 4)
+    assert U.shape == (3, 16, 16, 16)
+    # every fine cell holds the centroid of the leaf that covers it
+    fine = (np.stack(np.meshgrid(*[np.arange(16)] * 3, indexing="ij"), -1) + 0.5) / 16
+    hl = 0.5 / (1 << (np.where(fine[..., 0] < 0.25, 4, np.where(fine[..., 0] < 0.5, 3, 2)) - 1))
+    exp = (np.floor(fine / hl[..., None]) + 0.5) * hl[..., None]
+    assert np.allclose(np.moveaxis(U, 0, -1), exp)
