@@ -383,24 +383,36 @@ def measure_fp32_form(mesh, S0, dt, kw, args, dev, fp64_solver) -> dict:
                 per_kernel.setdefault(name, []).append(ms)
     mean_ms = {k: sum(v) / len(v) for k, v in per_kernel.items()}
 
-    def advance(solver, S):
-        solver.upload_state(S)
-        solver.step(dt, args.steps)
-        return solver.download_state()
-
     mu = kw.get("mu")
     solid = 0 if mu is not None and mu[0] != 0.0 else None
-    ref = advance(fp64_solver, S0)
-    err = error_report(advance(s32, S0), ref, kw["gamma"], kw["pinf"], mu, kw["amin"], solid)
+    # error growth: the FP32 form and the FP64 form from a perturbed initial state, each
+    # against the FP64 form, at a few step counts (three solvers advanced side by side)
     rng = np.random.default_rng(20261203)
     Sp = S0 * (1.0 + FP32_PERTURBATION * rng.uniform(-1.0, 1.0, S0.shape))
-    floor = error_report(advance(fp64_solver, Sp), ref, kw["gamma"], kw["pinf"], mu, kw["amin"],
-                         solid)
+    sper = Solver(device=dev.index, precision=0, **kw)
+    sper.set_mesh(mesh)
+    for s, S in ((fp64_solver, S0), (s32, S0), (sper, Sp)):
+        s.upload_state(S)
+    growth, done = [], 0
+    for c in sorted({min(5, args.steps), min(10, args.steps), args.steps}):
+        for s in (fp64_solver, s32, sper):
+            s.step(dt, c - done)
+        done = c
+        ref = fp64_solver.download_state()
+        e32 = error_report(s32.download_state(), ref, kw["gamma"], kw["pinf"], mu, kw["amin"],
+                           solid)
+        efl = error_report(sper.download_state(), ref, kw["gamma"], kw["pinf"], mu, kw["amin"],
+                           solid)
+        growth.append({"steps": c, "fp32_form": e32, "fp64_perturbed": efl})
+        del ref
+    sper.close()
+    err, floor = growth[-1]["fp32_form"], growth[-1]["fp64_perturbed"]
     s32.close()
     return {"value": mesh.n * args.steps / (t_ms / 1e3), "unit": UNIT,
             "ms_per_step": t_ms / args.steps, "kernel_mean_ms_per_stage": mean_ms,
             "error_vs_fp64": err, "error_steps": args.steps,
             "fp64_sensitivity_floor": {"perturbation": FP32_PERTURBATION, **floor},
+            "error_growth": growth,
             "note": "error of the FP32-flux form against the FP64 form after error_steps steps, "
                     "beside the FP64 form's own change when its initial state is perturbed by "
                     "1e-7 relative: the reference's model-5 scheme amplifies rounding-level "

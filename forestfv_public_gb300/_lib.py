@@ -77,10 +77,10 @@ EXPORTS = (
     "ffv_destroy", "ffv_set_mesh", "ffv_upload_state", "ffv_download_state", "ffv_stage",
     "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
     "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
-    "ffv_tags", "ffv_tags_raw", "ffv_tags_missed", "ffv_tags_smooth", "ffv_adapt", "ffv_mesh_leaves",
+    "ffv_tags", "ffv_tags_raw", "ffv_tags_missed", "ffv_tags_smooth", "ffv_adapt", "ffv_adapt_map", "ffv_adapt_changes", "ffv_mesh_leaves",
     "ffv_mlp_create", "ffv_mlp_destroy", "ffv_mlp_get_params", "ffv_mlp_set_params",
     "ffv_mlp_set_norm", "ffv_mlp_fields", "ffv_mlp_features", "ffv_mlp_forward",
-    "ffv_mlp_predict", "ffv_mlp_grad", "ffv_mlp_train",
+    "ffv_mlp_predict", "ffv_mlp_mark", "ffv_mlp_grad", "ffv_mlp_train",
 )
 
 
@@ -122,6 +122,8 @@ def lib() -> ctypes.CDLL:
     L.ffv_tags_smooth.argtypes = [vp, i32, vp]
     L.ffv_adapt.argtypes = [vp, vp, vp, ctypes.POINTER(vp)]
     L.ffv_mesh_leaves.argtypes = [vp, vp, vp, vp]
+    L.ffv_adapt_map.argtypes = [vp, vp, vp, ctypes.POINTER(vp), vp]
+    L.ffv_adapt_changes.argtypes = [vp, vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]
     u64, f32 = ctypes.c_uint64, ctypes.c_float
     L.ffv_mlp_create.argtypes = [ctypes.POINTER(vp), ctypes.c_int, u64]
     L.ffv_mlp_destroy.argtypes = [vp]
@@ -132,6 +134,7 @@ def lib() -> ctypes.CDLL:
     L.ffv_mlp_features.argtypes = [vp, vp, vp]
     L.ffv_mlp_forward.argtypes = [vp, vp, i64, vp]
     L.ffv_mlp_predict.argtypes = [vp, vp, vp]
+    L.ffv_mlp_mark.argtypes = [vp, vp, f32, vp, i32]
     L.ffv_mlp_grad.argtypes = [vp, vp, vp, i64, vp, vp]
     L.ffv_mlp_train.argtypes = [vp, vp, vp, i64, i32, i32, f32, f32, u64, vp]
     L.ffv_error_string.argtypes = [ctypes.c_int]

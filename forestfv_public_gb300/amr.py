@@ -59,37 +59,19 @@ class AMRStats:
                 "cell_updates_per_s": self.cell_updates / max(self.seconds, 1e-30)}
 
 
-_DEPTH = 20  # Morton digits of a leaf key below the tree (levels up to 21)
-
-
-def morton_intervals(mesh) -> tuple[np.ndarray, np.ndarray]:
-    """[start, end) of every leaf on one Morton line: the tree's rank in leaf order, then
-    the child-index digits of the leaf (corner k at (bit1 k, bit0 k, bit2 k)).  Leaf order
-    is increasing start order."""
-    from .mesh import _spread3, morton_tree_order
-    order = morton_tree_order(mesh.ntrees)
-    T = np.asarray(mesh.ntrees, np.int64)
-    rank_of = np.empty(int(T.prod()), np.int64)
-    rank_of[(order[:, 0] * T[1] + order[:, 1]) * T[2] + order[:, 2]] = np.arange(len(order))
-    t = mesh.tree_ijk.astype(np.int64)
-    rank = rank_of[(t[:, 0] * T[1] + t[:, 1]) * T[2] + t[:, 2]].astype(np.uint64)
-    c = mesh.cell_ijk
-    key = (_spread3(c[:, 0]) << np.uint64(1)) | _spread3(c[:, 1]) | (_spread3(c[:, 2]) << np.uint64(2))
-    shift = (3 * (_DEPTH - (mesh.level.astype(np.int64) - 1))).astype(np.uint64)
-    start = (rank << np.uint64(3 * _DEPTH)) | (key << shift)
-    return start, start + (np.uint64(1) << shift)
-
-
-def carry_marks(old, marks: np.ndarray, new) -> np.ndarray:
-    """Marks of the leaves of `old` carried to the leaves of `new` (same forest): a new leaf
-    is marked when it overlaps a marked old leaf -- children inherit their parent's mark, a
-    merged parent any of its children's."""
-    a0, _ = morton_intervals(old)
-    a1, b1 = morton_intervals(new)
-    lo = np.searchsorted(a0, a1, side="right") - 1
-    hi = np.searchsorted(a0, b1, side="left") - 1
-    csum = np.concatenate([[0], np.cumsum(marks.astype(np.int64))])
-    return (csum[hi + 1] - csum[lo]) > 0
+def carry_marks(src: np.ndarray, marks: np.ndarray) -> np.ndarray:
+    """Marks of the old leaves carried to the new leaves of a refineh pass, given every new
+    leaf's source (ffv_adapt_map): a kept leaf or a child keeps its (parent's) mark, a
+    merged parent takes any of its eight children's."""
+    out = np.empty(src.shape[0], bool)
+    keep = src >= 0
+    out[keep] = marks[src[keep]]
+    j = -1 - src[~keep]
+    acc = np.zeros(j.shape[0], bool)
+    for q in range(8):
+        acc |= marks[j + q]
+    out[~keep] = acc
+    return out
 
 
 def gradient_level(params) -> int:
@@ -131,24 +113,32 @@ class AdaptiveRun:
             rounds += 1
         return rounds
 
-    def _predict_marks(self) -> np.ndarray:
-        return self.indicator.predict(self.solver) > self.threshold
+    def _mark(self, accumulate: bool) -> None:
+        """Run the network and OR its marks into the device buffer (no copy back)."""
+        import torch
+        n = self.solver.mesh.n
+        if self.marks is None or self.marks.shape[0] != n:
+            # no fill: the first mark overwrites every entry (and a fill on torch's stream
+            # would race with the mark kernel on the solver's)
+            self.marks = torch.empty(n, dtype=torch.uint8, device=f"cuda:{self.indicator.device}")
+            accumulate = False
+        self.indicator.mark(self.solver, self.threshold, self.marks, accumulate)
 
     def learned_regrid(self) -> int:
         """A regrid whose target is the criterion's, raised to pre_level on marked cells."""
         s, rounds = self.solver, 0
-        marks = self.marks
-        if marks is None or marks.shape[0] != s.mesh.n:
-            marks = self._predict_marks()
+        if self.marks is None or self.marks.shape[0] != s.mesh.n:
+            self._mark(accumulate=False)
+        s.sync()
+        marks = self.marks.cpu().numpy().astype(bool)
         for _ in range(self.lmax + 1):
             raw = s.tags_raw(self.params)
             tgt = np.where(marks, np.maximum(raw, self.pre_level), raw).astype(np.int32)
             tgt = tags_smooth(s.mesh, self.lmax, tgt)
             if not would_change(s.mesh, tgt):
                 break
-            old = s.mesh
-            s.adapt(tgt)
-            marks = carry_marks(old, marks, s.mesh)
+            _, src = s.adapt(tgt, with_src=True)
+            marks = carry_marks(src, marks)
             rounds += 1
         self.marks = None
         return rounds
@@ -181,8 +171,7 @@ class AdaptiveRun:
                         st.skipped += 1
             if self.indicator is not None and k % self.infer_every == 0:
                 t0 = time.perf_counter()
-                m = self._predict_marks()
-                self.marks = m if self.marks is None or self.marks.shape != m.shape else (self.marks | m)
+                self._mark(accumulate=True)
                 st.t_infer += time.perf_counter() - t0
             t0 = time.perf_counter()
             s.step(dt, 1)

@@ -52,7 +52,8 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves, cons
 extern "C" void ffv_mesh_free(ffv_mesh *m);
 int ffv_ctx_mark_state(ffv_ctx *ctx);
 
-extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **out) {
+extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split,
+                             ffv_mesh **out, int64_t *src) {
   if (!ctx || !m || !split || !out) return FFV_ERR_ARG;
   *out = nullptr;
   int device, neq, model;
@@ -111,6 +112,7 @@ extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, 
   if (rc != FFV_OK) return rc;
   std::vector<int64_t> cmap(n_new);
   for (int64_t j = 0; j < n_new; j++) cmap[j] = map[order[j]];
+  if (src) memcpy(src, cmap.data(), sizeof(int64_t) * n_new);
   // carry the state over on the device, then swap the tables
   cudaError_t e = cudaSetDevice(device);
   int64_t *d_map = nullptr;
@@ -150,6 +152,10 @@ extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, 
   }
   *out = nm;
   return FFV_OK;
+}
+
+extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **out) {
+  return ffv_adapt_map(ctx, m, split, out, nullptr);
 }
 
 // the leaves of a mesh in its cell order (the inverse of ffv_mesh_build's input)

@@ -456,6 +456,16 @@ __global__ void __launch_bounds__(TPB) mlp_train_kernel(const bf16 *__restrict__
 }
 
 // AdamW (decoupled weight decay on W1, W2, w3; none on the biases)
+// marks[c] = (accumulate ? marks[c] : 0) | (prob[c] > threshold)
+__global__ void mlp_mark(int64_t n, const float *__restrict__ prob, float threshold,
+                         uint8_t *__restrict__ marks, int accumulate) {
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t hit = prob[c] > threshold ? 1 : 0;
+    marks[c] = accumulate ? (uint8_t)(marks[c] | hit) : hit;
+  }
+}
+
 __global__ void mlp_adamw(float *__restrict__ P, const float *__restrict__ G, float *__restrict__ M,
                           float *__restrict__ V, float lr, float wd, float b1, float b2, float eps,
                           float c1, float c2) {
@@ -738,6 +748,26 @@ int ffv_mlp_predict(ffv_ctx *ctx, ffv_mlp *m, float *prob_host) {
   if (rc != FFV_OK) return rc;
   MCK(cudaMemcpyAsync(prob_host, m->d_prob, sizeof(float) * v.dm.n, cudaMemcpyDeviceToHost, v.st));
   MCK(cudaStreamSynchronize(v.st));
+  return FFV_OK;
+}
+
+int ffv_mlp_mark(ffv_ctx *ctx, ffv_mlp *m, float threshold, uint8_t *marks_dev,
+                 int32_t accumulate) {
+  if (!m || !marks_dev) return FFV_ERR_ARG;
+  CtxView v;
+  int rc = view(ctx, v);
+  if (rc != FFV_OK) return rc;
+  if (v.device != m->device) return FFV_ERR_ARG;
+  MCK(cudaSetDevice(v.device));
+  rc = ensure_cap(m, v.dm.n);
+  if (rc != FFV_OK) return rc;
+  launch_fields(v, m->d_F);
+  mlp_gather<<<(unsigned)((v.dm.n + 127) / 128), 128, 0, v.st>>>(v.dm, m->d_F, m->d_norm, m->d_X);
+  MCK(cudaGetLastError());
+  rc = forward(m, m->d_X, v.dm.n, m->d_prob, v.st);
+  if (rc != FFV_OK) return rc;
+  mlp_mark<<<152 * 4, 256, 0, v.st>>>(v.dm.n, m->d_prob, threshold, marks_dev, accumulate);
+  MCK(cudaGetLastError());
   return FFV_OK;
 }
 

@@ -20,10 +20,14 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   std::vector<int64_t> group(n);
   for (int64_t c = 0; c < n; c++) group[c] = ffv_sibling_group(m, c);
   auto level = [&](int64_t c) { return (int32_t)ffv_info_level(m->info[c]); };
+  // A pass is a function of `split` alone: once one changes nothing, every later pass
+  // would see the same input and change nothing either, so the passes end there.
   for (int32_t pass = 0; pass < level_max + 1; pass++) {
+    bool changed = false;
     // criterionsmth.c:14-33: a leaf coarsens only with all eight siblings, refines by one
     for (int64_t c = 0; c < n; c++) {
       const int32_t l = level(c);
+      const int32_t before = split[c];
       if (l > 1) {
         // only leaf children count (criterionsmth.c:19-21): a group with a refined sibling
         // cannot reach eight
@@ -36,6 +40,7 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
         else if (l > split[c]) split[c] = l;
       }
       if (l < split[c]) split[c] = l + 1;
+      changed |= split[c] != before;
     }
     // criterionsmth.c:37-51: at most one level below any face neighbour
     for (int64_t c = 0; c < n; c++) {
@@ -51,8 +56,32 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
           mx = std::max(split[s], mx);
         }
       }
-      if (mx - split[c] > 1) split[c] = mx - 1;
+      if (mx - split[c] > 1) {
+        split[c] = mx - 1;
+        changed = true;
+      }
+    }
+    if (!changed) break;
+  }
+  return FFV_OK;
+}
+
+// what one refineh pass (ffv_adapt) would do with these targets: leaves that split, and
+// complete groups of eight sibling leaves that merge (refineh.c:10-57)
+extern "C" int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit,
+                                 int64_t *nmerge) {
+  if (!m || !split || !nsplit || !nmerge) return FFV_ERR_ARG;
+  int64_t ns = 0, nm = 0;
+  for (int64_t c = 0; c < m->n; c++) {
+    const int32_t l = (int32_t)ffv_info_level(m->info[c]);
+    if (split[c] > l) ns++;
+    if (l > 1 && ffv_sibling_group(m, c) == c) {
+      bool all = true;
+      for (int q = 0; q < 8 && all; q++) all = split[c + q] < l;
+      nm += all ? 1 : 0;
     }
   }
+  *nsplit = ns;
+  *nmerge = nm;
   return FFV_OK;
 }

@@ -83,6 +83,13 @@ class Indicator:
                    "ffv_mlp_predict")
         return p
 
+    def mark(self, solver, threshold: float, marks, accumulate: bool) -> None:
+        """marks (device uint8 tensor [n]) |= probability > threshold, on the solver's
+        stream, nothing copied back (ffv_mlp_mark)."""
+        _lib.check(_lib.lib().ffv_mlp_mark(solver._h, self._h, float(threshold),
+                                           marks.data_ptr(), 1 if accumulate else 0),
+                   "ffv_mlp_mark")
+
     def grad(self, X, y, B: int | None = None):
         B = X.shape[0] if B is None else B
         g = np.empty(NPARAM, np.float32)

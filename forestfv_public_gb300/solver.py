@@ -24,27 +24,21 @@ def level_max(params) -> int:
                params.lvl_inter0, params.lvl_inter1)
 
 
+def adapt_changes(mesh: Mesh, split: np.ndarray) -> tuple[int, int]:
+    """(leaves that split, sibling groups that merge) in a refineh pass with targets
+    `split` (ffv_adapt_changes, host)."""
+    split = np.ascontiguousarray(split, dtype=np.int32)
+    ns, nm = ctypes.c_int64(), ctypes.c_int64()
+    _lib.check(_lib.lib().ffv_adapt_changes(mesh.handle, split.ctypes.data, ctypes.byref(ns),
+                                            ctypes.byref(nm)), "ffv_adapt_changes")
+    return int(ns.value), int(nm.value)
+
+
 def would_change(mesh: Mesh, split: np.ndarray) -> bool:
     """Whether a refineh pass with targets `split` changes any leaf: a leaf wants a finer
-    level, or eight sibling leaves (consecutive, child indices 0..7, one parent) all want a
-    coarser one (refineh.c:10-57)."""
-    lev = mesh.level
-    if np.any(split > lev):
-        return True
-    low = split < lev
-    if not low.any():
-        return False
-    c = mesh.cell_ijk
-    kid = ((c[:, 0] & 1) << 1) | (c[:, 1] & 1) | ((c[:, 2] & 1) << 2)
-    s = np.flatnonzero(low & (kid == 0) & (lev > 1))
-    s = s[s + 7 < lev.size]
-    ok = np.ones(s.size, bool)
-    for q in range(1, 8):
-        j = s + q
-        ok &= (low[j] & (kid[j] == q) & (lev[j] == lev[s])
-               & np.all(mesh.tree_ijk[j] == mesh.tree_ijk[s], axis=1)
-               & np.all((c[j] >> 1) == (c[s] >> 1), axis=1))
-    return bool(ok.any())
+    level, or eight sibling leaves all want a coarser one (refineh.c:10-57)."""
+    ns, nm = adapt_changes(mesh, split)
+    return ns + nm > 0
 
 
 def tags_smooth(mesh: Mesh, lmax: int, split: np.ndarray) -> np.ndarray:
@@ -146,16 +140,26 @@ class Solver:
                                               ctypes.byref(out)), "ffv_tags_missed")
         return int(out.value)
 
-    def adapt(self, split) -> Mesh:
+    def adapt(self, split, with_src: bool = False):
         """One refineh pass (ffv_adapt) with target levels `split`; the solver continues on
-        the returned mesh with the carried-over state."""
+        the returned mesh with the carried-over state.  with_src also returns every new
+        leaf's source (ffv_adapt_map: the old leaf it copies, or -1 - j for a parent merged
+        from old leaves j..j+7)."""
         split = np.ascontiguousarray(split, dtype=np.int32)
         assert split.shape == (self.mesh.n,)
         h = ctypes.c_void_p()
-        _lib.check(_lib.lib().ffv_adapt(self._h, self.mesh.handle, split.ctypes.data,
-                                        ctypes.byref(h)), "ffv_adapt")
+        src = None
+        if with_src:
+            ns, nm = adapt_changes(self.mesh, split)
+            src = np.empty(self.mesh.n + 7 * (ns - nm), np.int64)
+        _lib.check(_lib.lib().ffv_adapt_map(self._h, self.mesh.handle, split.ctypes.data,
+                                            ctypes.byref(h),
+                                            src.ctypes.data if with_src else None), "ffv_adapt")
         old = self.mesh
         self.mesh = Mesh.from_handle(h, old.ntrees, old.bc, old.tree_edge)
+        if with_src:
+            assert src.shape[0] == self.mesh.n
+            return self.mesh, src
         return self.mesh
 
     def meshadaptation(self, params) -> Mesh:

@@ -200,6 +200,14 @@ int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *split);
  * its tables and the carried-over state.  The reference's meshadaptation is LEVEL + 1 rounds
  * of ffv_tags + ffv_adapt. */
 int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **out);
+/* ffv_adapt, and src[n_new] (nullable) receives the source of every new leaf: the old
+ * leaf it copies or splits from (>= 0), or -1 - j for a parent merged from the old leaves
+ * j..j+7.  n_new = n + 7 (nsplit - nmerge) with the counts of ffv_adapt_changes. */
+int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **out,
+                  int64_t *src);
+/* What one refineh pass with targets split[n] would do (host, no GPU): the number of
+ * leaves that split and of sibling groups that merge.  Both 0: the pass changes nothing. */
+int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit, int64_t *nmerge);
 /* The leaves of a mesh in its cell order (tree_ijk[3n], level[n], cell_ijk[3n]). */
 int ffv_mesh_leaves(const ffv_mesh *m, int32_t *tree_ijk, int32_t *level, int32_t *cell_ijk);
 
@@ -226,6 +234,11 @@ int ffv_mlp_features(ffv_ctx *ctx, ffv_mlp *mlp, void *X_dev);
 int ffv_mlp_forward(ffv_mlp *mlp, const void *X_dev, int64_t n, float *prob_dev);
 /* features + forward of the context's state, probabilities to the host (n) */
 int ffv_mlp_predict(ffv_ctx *ctx, ffv_mlp *mlp, float *prob_host);
+/* The network on the context's state, on the context's stream with no copy back:
+ * marks_dev[c] (device, uint8 [n]) becomes 1 where the probability exceeds threshold, OR-ed
+ * into its previous value when accumulate is nonzero. */
+int ffv_mlp_mark(ffv_ctx *ctx, ffv_mlp *mlp, float threshold, uint8_t *marks_dev,
+                 int32_t accumulate);
 /* gradient (host, FFV_MLP_NPARAM) and loss of the mean binary cross-entropy over the first
  * B rows of X_dev / labels y_dev (device, FP32 0 or 1) */
 int ffv_mlp_grad(ffv_mlp *mlp, const void *X_dev, const float *y_dev, int64_t B,
