@@ -27,6 +27,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 SOURCES = {
     "ffv_mesh.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "ffv_tags.cpp": [],
+    "ffv_io.cpp": [],
     "ffv_api.cu": [],
     "ffv_m0_fp64.cu": ["--fmad=false"],
     "ffv_m5_fp64.cu": ["--fmad=false"],

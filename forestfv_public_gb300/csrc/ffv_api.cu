@@ -252,6 +252,7 @@ const char *ffv_error_string(int code) {
     case FFV_ERR_NOMEM: return "out of memory";
     case FFV_ERR_STATE: return "call out of order";
     case FFV_ERR_TOO_LARGE: return "mesh larger than the no-allocation scratch";
+    case FFV_ERR_IO: return "file cannot be read or written, or is corrupt";
     default: return "unknown error";
   }
 }
@@ -610,6 +611,19 @@ int ffv_tags(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *sp
   CK(cudaStreamSynchronize(c->stream));
   if (split_raw) memcpy(split_raw, split, sizeof(int32_t) * n);
   return ffv_tags_smooth(m, level_max, split);
+}
+
+int ffv_export_fields(ffv_ctx *c, double *F_dev, int32_t *nf) {
+  if (!c || !nf) return FFV_ERR_ARG;
+  *nf = c->p.model == 5 ? 5 + 2 * c->p.nmaterials + 1 : 5;
+  if (!F_dev) return FFV_OK;
+  if (!c->have_state) return FFV_ERR_STATE;
+  CK(cudaSetDevice(c->device));
+  if (c->p.model == 5) ffv_m5_export_fields(c->n, c->m5, c->d_S, F_dev, c->stream);
+  else ffv_m0_export_fields(c->n, c->p.gamma[0], c->p.pinf[0], c->d_S, F_dev, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return FFV_OK;
 }
 
 int ffv_tags_raw(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t *split_raw,

@@ -80,7 +80,26 @@ __global__ void __launch_bounds__(128) m0_indicator_fields(int64_t n, double gam
   F[4 * n + c] = 0.0f;
 }
 
+__global__ void __launch_bounds__(128) m0_export_fields(int64_t n, double gamma, double pinf,
+                                                        const double *__restrict__ S,
+                                                        double *__restrict__ F) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double r, p, um;
+  m0_prim(S, n, c, gamma, pinf, r, p, um);
+  F[c] = r;
+  F[n + c] = -S[n + c] / r;  // the state holds the negated momentum in this node layout
+  F[2 * n + c] = -S[2 * n + c] / r;
+  F[3 * n + c] = -S[3 * n + c] / r;
+  F[4 * n + c] = p;
+}
+
 }  // namespace
+
+void ffv_m0_export_fields(int64_t n, double gamma, double pinf, const double *S, double *F,
+                          cudaStream_t st) {
+  m0_export_fields<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(n, gamma, pinf, S, F);
+}
 
 void ffv_m0_tags(const ffv_dmesh &m, double gamma, double pinf, const ffv_m5_tagc &t,
                  const double *S, int32_t *split, cudaStream_t st) {

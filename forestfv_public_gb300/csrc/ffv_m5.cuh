@@ -74,6 +74,10 @@ void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, co
                  int32_t *SI, int32_t *SItmp, int32_t *split, cudaStream_t st);
 
 // fields of the learned refinement indicator, F [5][n] float (ffv_mlp.cu gathers them)
+void ffv_m5_export_fields(int64_t n, const M5Consts &k, const double *S, double *F,
+                          cudaStream_t st);
+void ffv_m0_export_fields(int64_t n, double gamma, double pinf, const double *S, double *F,
+                          cudaStream_t st);
 void ffv_m5_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
                              cudaStream_t st);
 

@@ -1485,6 +1485,44 @@ __global__ void __launch_bounds__(128) m5_indicator_fields(int64_t n, M5Consts k
   F[4 * n + c] = (float)sqrt(1.5 * j2);
 }
 
+// exported fields (FP64): rho, u, v, w, sum_k alpha_k p_k, alpha_k, p_k, von Mises stress
+// of the reference's cell primitives (make_sol of the cell state)
+template <int N>
+__global__ void __launch_bounds__(128) m5_export_fields(int64_t n, M5Consts k,
+                                                        const double *__restrict__ S,
+                                                        double *__restrict__ F) {
+  using C = K5<N>;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double s[C::NEQ];
+  load_state<N>(S, n, c, s);
+  Sol<N> q;
+  make_sol<N>(k, s, s, false, q);
+  double p = 0.0;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) p += q.avf[iv] * q.p[iv];
+  const double tr = (q.st[0][0] + q.st[1][1] + q.st[2][2]) / 3.0;
+  double j2 = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const double d = q.st[i][j] - (i == j ? tr : 0.0);
+      j2 += d * d;
+    }
+  F[c] = q.r;
+  F[n + c] = -q.u;  // the state holds the negated momentum in this node layout
+  F[2 * n + c] = -q.v;
+  F[3 * n + c] = -q.w;
+  F[4 * n + c] = p;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) {
+    F[(int64_t)(5 + iv) * n + c] = q.avf[iv];
+    F[(int64_t)(5 + N + iv) * n + c] = q.p[iv];
+  }
+  F[(int64_t)(5 + 2 * N) * n + c] = sqrt(1.5 * j2);
+}
+
 // merged cells of a mesh adaptation (map < 0): the reference's relaxation of the merged
 // state (merge.c:52-57)
 template <int N>
@@ -1508,6 +1546,13 @@ void ffv_m5_relax_merged(int64_t n, const M5Consts &k, const int64_t *map, doubl
   const unsigned gc = (unsigned)((n + 127) / 128);
   if (k.nmat == 2) m5_relax_merged<2><<<gc, 128, 0, st>>>(n, k, map, S);
   else m5_relax_merged<3><<<gc, 128, 0, st>>>(n, k, map, S);
+}
+
+void ffv_m5_export_fields(int64_t n, const M5Consts &k, const double *S, double *F,
+                          cudaStream_t st) {
+  const unsigned gc = (unsigned)((n + 127) / 128);
+  if (k.nmat == 2) m5_export_fields<2><<<gc, 128, 0, st>>>(n, k, S, F);
+  else m5_export_fields<3><<<gc, 128, 0, st>>>(n, k, S, F);
 }
 
 void ffv_m5_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,

@@ -72,6 +72,7 @@ class Solver:
         h = ctypes.c_void_p()
         _lib.check(L.ffv_create(ctypes.byref(h), ctypes.byref(p), device), "ffv_create")
         self._h = h
+        self.device = device
         self.mesh: Mesh | None = None
 
     def set_mesh(self, mesh: Mesh) -> None:

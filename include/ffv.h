@@ -47,6 +47,7 @@ extern "C" {
 #define FFV_ERR_NOMEM 9        /* host or device allocation failed                       */
 #define FFV_ERR_STATE 10       /* call out of order (e.g. step before mesh/state upload) */
 #define FFV_ERR_TOO_LARGE 11   /* mesh larger than the fixed scratch of ffv_step_noalloc */
+#define FFV_ERR_IO 12          /* file cannot be opened, read or written, or is corrupt  */
 
 #define FFV_MAX_MATERIALS 8
 #define FFV_MAX_NEQ 32
@@ -210,6 +211,41 @@ int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mes
 int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit, int64_t *nmerge);
 /* The leaves of a mesh in its cell order (tree_ijk[3n], level[n], cell_ijk[3n]). */
 int ffv_mesh_leaves(const ffv_mesh *m, int32_t *tree_ijk, int32_t *level, int32_t *cell_ijk);
+
+/* Checkpoint/restart and field export (host side, no GPU).
+ *
+ * Binary checkpoint (no counterpart in the reference): the leaves Morton-keyed (tree rank,
+ * level, child-index path) and the SoA FP64 state [neq][n] in the mesh's cell order, with an
+ * FNV-1a hash; bit-exact.  Read it back with ffv_checkpoint_info (sizes, forest) and
+ * ffv_checkpoint_read (mesh and state; S may be NULL).  A corrupt or truncated file gives
+ * FFV_ERR_IO. */
+int ffv_checkpoint_write(const char *path, const ffv_mesh *m, const double *S, int32_t neq,
+                         int64_t istep, double time);
+int ffv_checkpoint_info(const char *path, ffv_forest_desc *desc, int64_t *n, int32_t *neq,
+                        int64_t *istep, double *time);
+int ffv_checkpoint_read(const char *path, ffv_mesh **out, double *S);
+/* The reference's text restart file (restart_save.c:13-50 writes it, restart_load.c:13-45
+ * reads it): header "istep time nleaves ntrees neq", one line per leaf "root tag S..." with
+ * "%15.10e" values.  The write is byte-identical to the reference's for the same leaves and
+ * state (levels up to 10: tags are 32-bit base-10 numbers); the read takes the forest's
+ * tree counts and boundary codes from desc (the file has only the total tree count). */
+int ffv_restart_text_write(const char *path, const ffv_mesh *m, const double *S, int32_t neq,
+                           int64_t istep, double time);
+int ffv_restart_text_info(const char *path, int64_t *n, int32_t *neq, int64_t *istep, double *time,
+                          int32_t *ntrees_total);
+int ffv_restart_text_read(const char *path, const ffv_forest_desc *desc, ffv_mesh **out,
+                          double *S);
+/* Tecplot ASCII export of per-leaf fields (headless; the reference's m5_exportfield_linked.c
+ * writes node-averaged fields of the same kind): one FEBRICK zone whose nodes are shared
+ * between leaves on the finest level's lattice, F [nfields][n] cell-centred in BLOCK form. */
+int ffv_tecplot_write(const char *path, const ffv_mesh *m, int32_t nfields, const char *const *names,
+                      const double *F, double time);
+/* Per-leaf fields of the context's state into F_dev (device, FP64 [nf][n]; *nf receives nf):
+ * model 5: density, velocity u v w (physical: the state holds the negated momentum in this
+ * forest's node layout), mixture pressure sum_k alpha_k p_k, the N volume
+ * fractions, the N material pressures and the von Mises equivalent of the mixture stress
+ * (nf = 5 + 2 N + 1); model 0: density, u, v, w, pressure (nf = 5).  F_dev NULL: only nf. */
+int ffv_export_fields(ffv_ctx *ctx, double *F_dev, int32_t *nf);
 
 /* Learned refinement indicator (no counterpart in the reference): a 135-64-64-1
  * perceptron with GELU hidden layers and a sigmoid output over the 27-cell stencil of five

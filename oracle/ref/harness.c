@@ -301,6 +301,13 @@ void __wrap_loop(struct RUN *run) {
   __real_loop(run);
   double t1 = MPI_Wtime();
   dump(run, "final", t1 - t0, (int64_t)NSTEP + 1);
+  /* <case>.restart present: the reference's own restart file of the final state
+   * (restart_save.c, restart%08d.dat in the working directory) */
+  FILE *rf = open_case_file(run, ".restart");
+  if (rf) {
+    fclose(rf);
+    restart_save(run);
+  }
   tag_pass(run);
   adapt_pass(run);
 }

@@ -103,6 +103,8 @@ class Case:
     # criteria of the reference's own meshadaptation run on the final state (harness
     # .adapt file); the adapted leaf list comes back as the third dump
     adapt: tuple | None = None
+    # write the reference's own restart file of the final state (restart_save.c)
+    restart: bool = False
 
     @property
     def neq(self) -> int:
@@ -207,6 +209,9 @@ def write_case(c: Case, d: str, name: str = "case") -> str:
             for t in c.tags:
                 f.write(" ".join(repr(float(v)) if isinstance(v, float) else str(int(v))
                                  for v in t) + "\n")
+    if c.restart:
+        with open(base + ".restart", "w") as f:
+            f.write("1\n")
     if c.adapt is not None:
         with open(base + ".adapt", "w") as f:
             f.write(" ".join(repr(float(v)) if isinstance(v, float) else str(int(v))
@@ -242,6 +247,7 @@ class Dump:
     S: np.ndarray
     tags: np.ndarray | None = None  # [npass, n, 4]: SI[0], SI[1], split, smoothed split
     adapted: "Dump | None" = None  # the leaf list after the reference's meshadaptation
+    restart_text: str | None = None  # the reference's restart file of this state
 
 
 _LEAF_HDR = struct.Struct("<2i16i3dd2i")
@@ -300,6 +306,10 @@ def run_case(c: Case, workdir: str | None = None, timeout: float = 600.0):
                                        offset=12).reshape(npass, n, 4).copy()
         if os.path.exists(run + ".adapt.bin"):
             final.adapted = read_dump(run + ".adapt.bin")
+        rs = sorted(x for x in os.listdir(d) if x.startswith("restart") and x.endswith(".dat"))
+        if rs:
+            with open(os.path.join(d, rs[-1])) as f:
+                final.restart_text = f.read()
         return read_dump(run + ".init.bin"), final, r.stdout
     finally:
         if own:

@@ -7,7 +7,7 @@ small cases -- its per-leaf geometry (neighbours, areas, normals, distances, vol
 that the CPU restatement, the face-table builder and the CUDA path can be checked
 against the reference on a machine where the reference is not available.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py [fixture names]
 """
 from __future__ import annotations
 
@@ -88,6 +88,9 @@ TAG_PASSES = (
 )
 
 
+# the reference's own restart file (restart_save.c) of the final state of these cases
+RESTART = ("m0_sphere_amr", "m5_wall_amr")
+
 # the reference's meshadaptation on the final state of these cases (same criterion order)
 ADAPT = {
     "m5_bubble_prelax3": (1, 2, 0, 0, 0.0, 1, 5, 0.05, 0, 0, 0.0, 0, 0, 0, 0, 0, 0),
@@ -122,6 +125,8 @@ def save(name: str, c: rc.Case, keep_geom: bool) -> None:
     if final.tags is not None:
         d["tag_params"] = np.asarray(c.tags, dtype=np.float64)
         d["tags"] = final.tags.astype(np.int8)
+    if final.restart_text is not None:
+        d["restart_text"] = np.frombuffer(final.restart_text.encode("ascii"), dtype=np.uint8)
     if final.adapted is not None:
         a = final.adapted
         d.update(adapt_params=np.asarray(c.adapt, dtype=np.float64), adapt_root=a.root,
@@ -139,13 +144,19 @@ def save(name: str, c: rc.Case, keep_geom: bool) -> None:
 def main() -> None:
     if not rc.build_ref():
         raise SystemExit("reference oracle could not be built")
+    only = set(sys.argv[1:])  # optional: names of the fixtures to regenerate
     for name, (c, g) in CASES.items():
-        save(name, c, g)
+        if not only or name in only:
+            c.restart = name in RESTART
+            save(name, c, g)
     for name, c in M5_CASES.items():
-        c.tags = TAG_PASSES
-        c.adapt = ADAPT.get(name)
-        save(name, c, True)
-    save("m0_config1_sod32", config1_case(), False)
+        if not only or name in only:
+            c.tags = TAG_PASSES
+            c.adapt = ADAPT.get(name)
+            c.restart = name in RESTART
+            save(name, c, True)
+    if not only or "m0_config1_sod32" in only:
+        save("m0_config1_sod32", config1_case(), False)
 
 
 if __name__ == "__main__":
