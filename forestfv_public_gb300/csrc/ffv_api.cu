@@ -196,6 +196,10 @@ void ffv_fill_geom(const ffv_mesh *m, ffv_geom *g) {
     g->dcc[l][2] = 0.5 * h + 0.25 * h;
     g->dcf[l][3] = 0.0;
     g->dcc[l][3] = 0.0;
+    for (int q = 0; q < 4; q++) {
+      g->dcf_f[l][q] = (float)g->dcf[l][q];
+      g->idcc_f[l][q] = (float)(1.0 / g->dcc[l][q]);
+    }
   }
 }
 
@@ -313,9 +317,20 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
       // m5_relaxationvec.c's floor -(1 - 1e-8) p_inf + 1e-8 and reset value
       k.plo_f[i] = (float)(-(1.0 - 1.0e-8) * p->pinf[i] + 1.0e-8);
       k.preset_f[i] = (float)(-(1.0 - 1.0e-8) * p->pinf[i] + 1.0);
+      k.gm1_d[i] = df_from_double(gm1);
+      k.gpi_d[i] = df_from_double(k.gpi[i]);
+      k.ig1_d[i] = df_from_double(k.ig1[i]);
+      k.gpg_d[i] = df_from_double(k.gpg[i]);
+      k.pinf_d[i] = df_from_double(p->pinf[i]);
+      k.floor_d[i] = df_from_double(-(1.0 - 1.0e-8) * p->pinf[i] + 1.0e-8);
     }
     k.alo_f = (float)(p->amin / 100.0);
     k.ahi_f = (float)(1.0 - (p->amin / 100.0));
+    k.alo_d = df_from_double(p->amin / 100.0);
+    k.ahi_d = df_from_double(1.0 - (p->amin / 100.0));
+    k.a2lo_d = df_from_double(1.0 - (2.0 * (p->amin / 100.0)));
+    k.eps_d = df_from_double(1.0e-12);
+    k.oneeps_d = df_from_double(1.0 - 1.0e-12);
   }
   int rc = FFV_OK;
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||

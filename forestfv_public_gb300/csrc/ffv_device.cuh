@@ -31,6 +31,9 @@ struct ffv_geom {
   double h[FFV_MAX_LEVEL + 2];
   double dcf[FFV_MAX_LEVEL + 2][4];    // by face class: same, coarser, finer, boundary
   double dcc[FFV_MAX_LEVEL + 2][4];
+  // FP32 forms for the FP32-flux reconstruction: dcf and 1 / dcc (inf at a boundary)
+  float dcf_f[FFV_MAX_LEVEL + 2][4];
+  float idcc_f[FFV_MAX_LEVEL + 2][4];
 };
 
 __device__ __forceinline__ int face_class(uint32_t kind) { return (kind & FFV_FK_BC) ? 3 : (int)kind; }

@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include "ffv_device.cuh"
+#include "ffv_df.cuh"
 
 struct M5Consts {
   int nmat, order, prelax, nsolids;
@@ -20,6 +21,12 @@ struct M5Consts {
   float pinf_f[FFV_MAX_MATERIALS], igam_f[FFV_MAX_MATERIALS], mu_f[FFV_MAX_MATERIALS],
       gamma_f[FFV_MAX_MATERIALS], plo_f[FFV_MAX_MATERIALS], preset_f[FFV_MAX_MATERIALS];
   float alo_f, ahi_f;
+  // double-float pairs for the FP32-flux form's pressure recovery: gamma - 1, gamma p_inf,
+  // 1 / (gamma - 1), gamma p_inf / (gamma - 1), p_inf, the relaxation's pressure floor; and
+  // AMIN / 100, 1 - AMIN / 100, 1 - 2 AMIN / 100, 1e-12, 1 - 1e-12
+  df gm1_d[FFV_MAX_MATERIALS], gpi_d[FFV_MAX_MATERIALS], ig1_d[FFV_MAX_MATERIALS],
+      gpg_d[FFV_MAX_MATERIALS], pinf_d[FFV_MAX_MATERIALS], floor_d[FFV_MAX_MATERIALS];
+  df alo_d, ahi_d, a2lo_d, eps_d, oneeps_d;
 };
 
 struct ffv_m5_bufs {

@@ -717,13 +717,42 @@ __device__ void value_across_f(const M5Consts &k, const ffv_dmesh &m, const floa
   avf_limit_f<N>(k, X);
 }
 
-// the critical slots across face f (neighbour, mean of four finer, or the cell itself at
-// a boundary) in FP64, volume fractions limited as avf_limit does: their slopes are
-// differences of nearly equal numbers (a liquid fraction 1 - 1e-6, an energy of 1e9), which
-// the FP32 copy cannot resolve
+// the critical slots of cell o as double-float pairs: hi from the FP32 copy, lo from
+// Sflo [2N][n] (written with it by m5f_shadow)
 template <int N>
-__device__ void crit_across(const M5Consts &k, const ffv_dmesh &m, const double *__restrict__ S,
-                            int64_t c, int f, uint32_t kind, const double *own, double *X) {
+__device__ __forceinline__ void crit_load(const float *__restrict__ Sf, const float *__restrict__ Sflo,
+                                          int64_t n, int64_t o, df *X) {
+#pragma unroll
+  for (int j = 0; j < 2 * N; j++) X[j] = df{Sf[(int64_t)crit_slot<N>(j) * n + o], Sflo[(int64_t)j * n + o]};
+}
+
+// avf_limit.c:3-21 on the double-float volume fractions X[0..N-2]
+template <int N>
+__device__ __forceinline__ void avf_limit_df(const M5Consts &k, df *X) {
+  df sum = df_make(0.0f);
+#pragma unroll
+  for (int j = 0; j < N - 1; ++j) {
+    df a = X[j];
+    if (df_le(a, k.alo_d)) a = k.alo_d;
+    else if (df_le(k.ahi_d, a)) a = k.ahi_d;
+    X[j] = a;
+    sum = df_add(sum, a);
+  }
+  if (df_lt(k.ahi_d, sum)) {
+    const df dif = df_sub(sum, k.ahi_d);
+#pragma unroll
+    for (int j = 0; j < N - 1; ++j) X[j] = df_sub(X[j], df_mul(df_div(X[j], sum), dif));
+  }
+}
+
+// the critical slots across face f (neighbour, mean of four finer, or the cell itself at
+// a boundary), volume fractions limited as avf_limit does: their slopes are differences of
+// nearly equal numbers (a liquid fraction 1 - 1e-6, an energy of 1e9), which the FP32 copy
+// alone cannot resolve
+template <int N>
+__device__ void crit_across_df(const M5Consts &k, const ffv_dmesh &m, const float *__restrict__ Sf,
+                               const float *__restrict__ Sflo, int64_t c, int f, uint32_t kind,
+                               const df *own, df *X) {
   constexpr int NCR = 2 * N;
   if (kind & FFV_FK_BC) {
 #pragma unroll
@@ -732,77 +761,89 @@ __device__ void crit_across(const M5Consts &k, const ffv_dmesh &m, const double 
   }
   if (kind == FFV_FK_FINER) {
     const int32_t *sg = m.sub + 4 * (int64_t)m.nbr[(int64_t)f * m.n + c];
-#pragma unroll
-    for (int j = 0; j < NCR; j++) X[j] = 0.0;
+    crit_load<N>(Sf, Sflo, m.n, sg[0], X);
 #pragma unroll 1
-    for (int q = 0; q < 4; q++) {
-      const int64_t o = sg[q];
+    for (int q = 1; q < 4; q++) {
+      df Y[NCR];
+      crit_load<N>(Sf, Sflo, m.n, sg[q], Y);
 #pragma unroll
-      for (int j = 0; j < NCR; j++) X[j] += S[(int64_t)crit_slot<N>(j) * m.n + o];
+      for (int j = 0; j < NCR; j++) X[j] = df_add(X[j], Y[j]);
     }
 #pragma unroll
-    for (int j = 0; j < NCR; j++) X[j] *= 0.25;
+    for (int j = 0; j < NCR; j++) X[j] = df{X[j].hi * 0.25f, X[j].lo * 0.25f};
   } else {
-    const int64_t o = m.nbr[(int64_t)f * m.n + c];
-#pragma unroll
-    for (int j = 0; j < NCR; j++) X[j] = S[(int64_t)crit_slot<N>(j) * m.n + o];
+    crit_load<N>(Sf, Sflo, m.n, m.nbr[(int64_t)f * m.n + c], X);
   }
-  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
-  double sum = 0.0;
+  avf_limit_df<N>(k, X);
+}
+
+// vf_limit_relax_d in double-float: the N-1 fractions clamped (else-if or two ifs as the
+// reference's two call sites have it), renormalised when their sum reaches 1 - lo, the last
+// fraction 1 - sum
+template <int N>
+__device__ __forceinline__ void vf_limit_relax_df(const M5Consts &k, df *avf, bool elseif) {
+  df sum = df_make(0.0f);
 #pragma unroll
-  for (int j = 0; j < N - 1; ++j) {
-    double a = X[j];
-    if (a <= lo) a = lo;
-    else if (a >= hi) a = hi;
-    X[j] = a;
-    sum += a;
+  for (int i = 0; i < N - 1; ++i) {
+    if (elseif) {
+      if (df_le(avf[i], k.alo_d)) avf[i] = k.alo_d;
+      else if (df_le(k.ahi_d, avf[i])) avf[i] = k.ahi_d;
+    } else {
+      if (df_le(avf[i], k.alo_d)) avf[i] = k.alo_d;
+      if (df_le(k.ahi_d, avf[i])) avf[i] = k.ahi_d;
+    }
+    sum = df_add(sum, avf[i]);
   }
-  if (sum > hi) {
-    const double dif = sum - hi;
+  if (df_le(k.ahi_d, sum)) {
+    const df dif = df_sub(sum, k.ahi_d);
 #pragma unroll
-    for (int j = 0; j < N - 1; ++j) X[j] -= (X[j] / sum) * dif;
+    for (int j = 0; j < N - 1; ++j) avf[j] = df_sub(avf[j], df_mul(df_div(avf[j], sum), dif));
+    sum = k.ahi_d;
   }
+  avf[N - 1] = df_sub(df_make(1.0f), sum);
 }
 
 // m5_relaxationvec.c on a face state: FP32 partial densities, momentum and deformation in
-// v, FP64 critical slots in cr; the pressure recovery and the energy-consistent equilibrium
-// in FP64 with the materials' constants gamma p_inf / (gamma - 1), 1 / (gamma - 1) and
-// gamma p_inf formed once on the host; the Newton iteration as relax_mixed's
+// v, the critical slots in cr as double-float pairs; the pressure recovery and the
+// energy-consistent equilibrium in double-float, the Newton iteration as relax_mixed's in
+// FP32.  PRELAX 1 (the two-material closed form) converts to FP64 and back.
 template <int N>
-__device__ unsigned relax_face(const M5Consts &k, float *v, double *cr, double &p_out) {
+__device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_out) {
   using C = K5<N>;
-  double ar[N], are[N], avf[N], avf0[N], ael[N];
+  df ar[N], are[N], avf[N], avf0[N];
+  float ael[N];
   float rf = 0.0f;
 #pragma unroll
   for (int iv = 0; iv < N; ++iv) {
     rf += v[C::i0 + iv];
-    ar[iv] = (double)v[C::i0 + iv];
+    ar[iv] = df_make(v[C::i0 + iv]);
     are[iv] = cr[N - 1 + iv];
   }
-  const double rE = cr[2 * N - 1];
+  const df rE = cr[2 * N - 1];
   const float mx = v[C::i1], my = v[C::i1 + 1], mz = v[C::i1 + 2];
-  const double ke = (double)(0.5f * (mx * mx + my * my + mz * mz) / rf);
+  const float ke = 0.5f * (mx * mx + my * my + mz * mz) / rf;
 #pragma unroll
   for (int iv = 0; iv < N - 1; ++iv) avf[iv] = cr[iv];
-  vf_limit_relax_d<N>(k, avf, true);
+  vf_limit_relax_df<N>(k, avf, true);
 #pragma unroll
   for (int iv = 0; iv < N; ++iv) avf0[iv] = avf[iv];
   float G[9], Gmag;
   gmat_f(v + C::i5, G, Gmag);
 #pragma unroll
-  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, k.mu_f[iv]);
-  const double eps_sml = 1.0e-12, eps_big = 1.0e-8;
+  for (int iv = 0; iv < N; ++iv) ael[iv] = elastic_energy_f(G, Gmag, k.mu_f[iv]);
   unsigned st = 0;
   float ratio = 1.0f;
-  if (k.prelax == 1) {  // closed form for two materials
-    double t0[N], p0[N];
+  if (k.prelax == 1) {  // closed form for two materials, in FP64
+    double a[N], t0[N], p0[N];
 #pragma unroll
     for (int iv = 0; iv < N; ++iv) {
-      t0[iv] = avf[iv] / ar[iv];
-      p0[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) - k.gpi[iv];
+      a[iv] = (double)avf[iv].hi + (double)avf[iv].lo;
+      t0[iv] = a[iv] / (double)ar[iv].hi;
+      p0[iv] = ((k.gamma[iv] - 1.0) * (((double)are[iv].hi + (double)are[iv].lo) - (double)ael[iv]) /
+                a[iv]) - k.gpi[iv];
     }
     const double *ga = k.gamma, *pi = k.pinf;
-    const double w0 = avf[0] / ga[0], w1 = avf[1] / ga[1];
+    const double w0 = a[0] / ga[0], w1 = a[1] / ga[1];
     const double A_1 = w0 * (p0[0] + pi[0]) / (w0 + w1);
     const double A_2 = w1 * (p0[1] + pi[1]) / (w0 + w1);
     const double d = (A_2 - A_1 - (pi[1] - pi[0]));
@@ -810,51 +851,51 @@ __device__ unsigned relax_face(const M5Consts &k, float *v, double *cr, double &
     if (isnan(pe)) st |= FFV_ST_NAN;
 #pragma unroll
     for (int iv = 0; iv < N; ++iv)
-      avf[iv] = ar[iv] * t0[iv] * (p0[iv] + k.gpi[iv] + (ga[iv] - 1.0) * pe) /
-                (pe + k.gpi[iv] + (ga[iv] - 1.0) * pe);
-    vf_limit_relax_d<N>(k, avf, false);
-    ratio = (float)avf[0] / (float)avf0[0];
+      avf[iv] = df_from_double((double)ar[iv].hi * t0[iv] * (p0[iv] + k.gpi[iv] + (ga[iv] - 1.0) * pe) /
+                               (pe + k.gpi[iv] + (ga[iv] - 1.0) * pe));
+    vf_limit_relax_df<N>(k, avf, false);
+    ratio = df_to_float(avf[0]) / df_to_float(avf0[0]);
   } else {  // PRELAX 3
-    double pkinit[N];
 #pragma unroll
     for (int iv = 0; iv < N; ++iv) {
-      if (avf[iv] < 0.0 || ar[iv] < 0.0) {
-        avf[iv] = eps_sml;
-        ar[iv] = eps_sml;
-        are[iv] = eps_sml;
+      if (avf[iv].hi < 0.0f || ar[iv].hi < 0.0f) {
+        avf[iv] = k.eps_d;
+        ar[iv] = k.eps_d;
+        are[iv] = k.eps_d;
       }
-      if (avf[iv] >= 1.0) avf[iv] = 1.0 - eps_sml;
+      if (!df_lt(avf[iv], df_make(1.0f))) avf[iv] = k.oneeps_d;
     }
     bool irelax = true;
 #pragma unroll
     for (int iv = 0; iv < N; ++iv)
-      if (avf[iv] > 1.0 - eps_sml) irelax = false;
+      if (df_lt(k.oneeps_d, avf[iv])) irelax = false;
     if (irelax) {
-      double p0 = 0.0, sum0 = -1.0;
+      df p0 = df_make(0.0f), sum0 = df_make(-1.0f);
       float a0[N], pkf[N], pif[N], b0[N], ig[N], e[N], plo[N], preset[N];
+      bool live[N];
 #pragma unroll
       for (int iv = 0; iv < N; ++iv) {
-        if (avf[iv] > eps_sml) {
-          pkinit[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) - k.gpi[iv];
-          const double floor_p = -(1.0 - eps_big) * k.pinf[iv] + eps_big;
-          if (pkinit[iv] <= floor_p) pkinit[iv] = floor_p;
-          sum0 += avf[iv];
-        } else {
-          pkinit[iv] = 0.0;
+        df pk = df_make(0.0f);
+        live[iv] = df_lt(k.eps_d, avf[iv]);
+        if (live[iv]) {
+          pk = df_sub(df_div(df_mul(k.gm1_d[iv], df_sub(are[iv], df_make(ael[iv]))), avf[iv]),
+                      k.gpi_d[iv]);
+          if (df_le(pk, k.floor_d[iv])) pk = k.floor_d[iv];
+          sum0 = df_add(sum0, avf[iv]);
         }
-        p0 += avf[iv] * pkinit[iv];
-        a0[iv] = (float)avf[iv];
-        pkf[iv] = (float)pkinit[iv];
+        p0 = df_add(p0, df_mul(avf[iv], pk));
+        a0[iv] = df_to_float(avf[iv]);
+        pkf[iv] = df_to_float(pk);
         pif[iv] = k.pinf_f[iv];
-        // in FP64: at a material's pressure floor pk + p_inf is a few Pa beside 6e8
-        b0[iv] = (float)(1.0 / (pkinit[iv] + k.pinf[iv]));
+        // at a material's pressure floor pk + p_inf is a few Pa beside 6e8
+        b0[iv] = df_to_float(df_div(df_make(1.0f), df_add(pk, k.pinf_d[iv])));
         ig[iv] = k.igam_f[iv];
         plo[iv] = k.plo_f[iv];
         preset[iv] = k.preset_f[iv];
         e[iv] = 0.0f;
       }
-      const float F0 = (float)sum0;
-      float pf = (float)p0, F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
+      const float F0 = df_to_float(sum0);
+      float pf = df_to_float(p0), F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
 #pragma unroll 1
       for (int iter = 0; iter < 64; iter++) {
         const float step = F / dF;
@@ -868,7 +909,7 @@ __device__ unsigned relax_face(const M5Consts &k, float *v, double *cr, double &
         dF = 0.0f;
 #pragma unroll
         for (int iv = 0; iv < N; ++iv) {
-          if (avf[iv] > eps_sml) {
+          if (live[iv]) {
             const float x = (pf - pkf[iv]) * b0[iv];
             const float opx = x > -0.5f ? 1.0f + x : fmaxf((pf + pif[iv]) * b0[iv], 1.0e-30f);
             const float lx = x > -0.5f ? log1pf(x) : logf(opx);
@@ -886,49 +927,63 @@ __device__ unsigned relax_face(const M5Consts &k, float *v, double *cr, double &
       }
 #pragma unroll
       for (int iv = 0; iv < N; ++iv)
-        if (avf[iv] > eps_sml) avf[iv] = avf[iv] + avf[iv] * (double)e[iv];
-      vf_limit_relax_d<N>(k, avf, true);
+        if (live[iv]) avf[iv] = df_add(avf[iv], df_mul_f(avf[iv], e[iv]));
+      vf_limit_relax_df<N>(k, avf, true);
     }
-    const int i_as = ((avf[0] < avf[1]) && (k.mu[1] != 0.0)) ? 1 : 0;
-    ratio = (float)avf[i_as] / (float)avf0[i_as];
+    const int i_as = (df_lt(avf[0], avf[1]) && (k.mu[1] != 0.0)) ? 1 : 0;
+    ratio = df_to_float(avf[i_as]) / df_to_float(avf0[i_as]);
   }
-  double num = 0.0, den = 0.0, sael = 0.0;
+  df num = df_make(0.0f), den = df_make(0.0f);
+  float sael = 0.0f;
 #pragma unroll
   for (int iv = 0; iv < N; ++iv) {
-    num += avf[iv] * k.gpg[iv];
-    den += avf[iv] * k.ig1[iv];
+    num = df_add(num, df_mul(avf[iv], k.gpg_d[iv]));
+    den = df_add(den, df_mul(avf[iv], k.ig1_d[iv]));
     sael += ael[iv];
   }
-  const double p = (rE - ke - sael - num) / den;
+  const df p = df_div(df_sub(df_add_f(df_add_f(rE, -ke), -sael), num), den);
 #pragma unroll
   for (int iv = 0; iv < N - 1; ++iv) {
-    if (isnan(avf[iv])) st |= FFV_ST_NAN;
+    if (df_isnan(avf[iv])) st |= FFV_ST_NAN;
     cr[iv] = avf[iv];
   }
 #pragma unroll
   for (int iv = 0; iv < N; iv++) {
-    const double a2 = avf[iv] * (p + k.gpi[iv]) * k.ig1[iv] + ael[iv];
-    if (isnan(a2)) st |= FFV_ST_NAN;
+    const df a2 = df_add_f(df_mul(df_mul(avf[iv], df_add(p, k.gpi_d[iv])), k.ig1_d[iv]), ael[iv]);
+    if (df_isnan(a2)) st |= FFV_ST_NAN;
     cr[N - 1 + iv] = a2;
   }
 #pragma unroll
   for (int q = 0; q < 9; ++q) v[C::i5 + q] *= ratio;
-  p_out = p;
+  p_out = df_to_float(p);
   return st;
 }
 
 // ------------------------------------------------------------------------------ kernels
-// FP32 copy of the state for the reconstruction (made once per cell per stage)
-__global__ void m5f_shadow(int64_t count, const double *__restrict__ S, float *__restrict__ Sf) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
-       i += (int64_t)gridDim.x * blockDim.x)
-    Sf[i] = (float)S[i];
+// FP32 copy of the state for the reconstruction (made once per cell per stage), and the
+// low parts of the critical slots' double-float pairs: Sflo[j][c] = S - (double)(float)S
+template <int N>
+__global__ void __launch_bounds__(256) m5f_shadow(int64_t n, const double *__restrict__ S,
+                                                  float *__restrict__ Sf, float *__restrict__ Sflo) {
+  using C = K5<N>;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int v = 0; v < C::NEQ; v++) {
+      const double x = S[(int64_t)v * n + c];
+      const float h = (float)x;
+      Sf[(int64_t)v * n + c] = h;
+#pragma unroll
+      for (int j = 0; j < 2 * N; j++)
+        if (crit_slot<N>(j) == v) Sflo[(int64_t)j * n + c] = (float)(x - (double)h);
+    }
+  }
 }
 
 template <int N>
 __global__ void __launch_bounds__(128) m5f_recon_face(ffv_dmesh m, ffv_geom g, M5Consts k,
-                                                      const double *__restrict__ S,
                                                       const float *__restrict__ Sf,
+                                                      const float *__restrict__ Sflo,
                                                       float *__restrict__ SF,
                                                       unsigned *__restrict__ status) {
   using C = K5<N>;
@@ -942,51 +997,34 @@ __global__ void __launch_bounds__(128) m5f_recon_face(ffv_dmesh m, ffv_geom g, M
   const uint32_t info = m.info[c];
   const int l = ffv_info_level(info);
   const uint32_t kf = ffv_face_kind(info, f), ko = ffv_face_kind(info, fo);
-  float sl[C::NEQ], x[C::NEQ], df[C::NEQ];
+  float sl[C::NEQ], x[C::NEQ], df_[C::NEQ];
 #pragma unroll
   for (int i = 0; i < C::NEQ; i++) sl[i] = Sf[(int64_t)i * m.n + c];
   avf_limit_f<N>(k, sl);
-  // FP64 critical slots of the cell (volume fractions limited as avf_limit does)
-  double cr[NCR];
-#pragma unroll
-  for (int j = 0; j < NCR; j++) cr[j] = S[(int64_t)crit_slot<N>(j) * m.n + c];
-  {
-    const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
-    double sum = 0.0;
-#pragma unroll
-    for (int j = 0; j < N - 1; ++j) {
-      double a = cr[j];
-      if (a <= lo) a = lo;
-      else if (a >= hi) a = hi;
-      cr[j] = a;
-      sum += a;
-    }
-    if (sum > hi) {
-      const double dif = sum - hi;
-#pragma unroll
-      for (int j = 0; j < N - 1; ++j) cr[j] -= (cr[j] / sum) * dif;
-    }
-  }
+  // the critical slots of the cell (volume fractions limited as avf_limit does)
+  df cr[NCR];
+  crit_load<N>(Sf, Sflo, m.n, c, cr);
+  avf_limit_df<N>(k, cr);
   value_across_f<N>(k, m, Sf, c, f, kf, sl, x);
 #pragma unroll
-  for (int i = 0; i < C::NEQ; i++) df[i] = x[i] - sl[i];
+  for (int i = 0; i < C::NEQ; i++) df_[i] = x[i] - sl[i];
   value_across_f<N>(k, m, Sf, c, fo, ko, sl, x);
-  // the critical slots' differences in FP64
+  // the critical slots' differences in double-float, rounded to FP32
   float dfc[NCR], dbc[NCR];
   {
-    double xc[NCR];
-    crit_across<N>(k, m, S, c, f, kf, cr, xc);
+    df xc[NCR];
+    crit_across_df<N>(k, m, Sf, Sflo, c, f, kf, cr, xc);
 #pragma unroll
-    for (int j = 0; j < NCR; j++) dfc[j] = (float)(xc[j] - cr[j]);
-    crit_across<N>(k, m, S, c, fo, ko, cr, xc);
+    for (int j = 0; j < NCR; j++) dfc[j] = df_to_float(df_sub(xc[j], cr[j]));
+    crit_across_df<N>(k, m, Sf, Sflo, c, fo, ko, cr, xc);
 #pragma unroll
-    for (int j = 0; j < NCR; j++) dbc[j] = (float)(xc[j] - cr[j]);
+    for (int j = 0; j < NCR; j++) dbc[j] = df_to_float(df_sub(xc[j], cr[j]));
   }
 #pragma unroll
-  for (int j = 0; j < NCR; j++) df[crit_slot<N>(j)] = dfc[j];
-  const float idp = (float)(1.0 / g.dcc[l][face_class(kf)]);
-  const float idm = (float)(1.0 / g.dcc[l][face_class(ko)]);
-  const float cf = (float)g.dcf[l][face_class(kf)];
+  for (int j = 0; j < NCR; j++) df_[crit_slot<N>(j)] = dfc[j];
+  const float idp = g.idcc_f[l][face_class(kf)];
+  const float idm = g.idcc_f[l][face_class(ko)];
+  const float cf = g.dcf_f[l][face_class(kf)];
   float corr[C::NEQ];
 #pragma unroll
   for (int i = 0; i < C::NEQ; i++) {
@@ -995,64 +1033,62 @@ __global__ void __launch_bounds__(128) m5f_recon_face(ffv_dmesh m, ffv_geom g, M
     for (int j = 0; j < NCR; j++)
       if (i == crit_slot<N>(j)) db = dbc[j];
     float grad = 0.0f;
-    if (!(kf & FFV_FK_BC) && fabsf(df[i]) > 1e-10f && !(i >= C::i4 && i < C::i5)) {
-      const float sf = df[i] * idp, sb = -db * idm;
+    if (!(kf & FFV_FK_BC) && fabsf(df_[i]) > 1e-10f && !(i >= C::i4 && i < C::i5)) {
+      const float sf = df_[i] * idp, sb = -db * idm;
       if (sb * sf > 0.0f) grad = (fabsf(sb) > fabsf(sf)) ? sf : sb;
     }
     corr[i] = cf * grad;
     sl[i] += corr[i];  // the face value of the FP32 copy
   }
 #pragma unroll
-  for (int j = 0; j < NCR; j++) cr[j] += (double)corr[crit_slot<N>(j)];
+  for (int j = 0; j < NCR; j++) cr[j] = df_add_f(cr[j], corr[crit_slot<N>(j)]);
   // m5_reconctruct.c:144-179: volume-fraction limits of the face state
   {
-    const double lo = k.amin / 100.0;
-    double sum = 0.0;
+    df sum = df_make(0.0f);
 #pragma unroll
     for (int iv = 0; iv < N - 1; ++iv) {
-      double a = cr[iv];
-      if (a <= lo) a = lo;
-      else if (a >= (1.0 - (2.0 * lo))) a = 1.0 - (2.0 * lo);
+      df a = cr[iv];
+      if (df_le(a, k.alo_d)) a = k.alo_d;
+      else if (df_le(k.a2lo_d, a)) a = k.a2lo_d;
       cr[iv] = a;
-      sum += a;
+      sum = df_add(sum, a);
     }
-    if (sum >= (1.0 - lo)) {
-      const double dif = sum - (1.0 - lo);
+    if (df_le(k.ahi_d, sum)) {
+      const df dif = df_sub(sum, k.ahi_d);
 #pragma unroll
-      for (int j = 0; j < N - 1; ++j) cr[j] -= (cr[j] / sum) * dif;
+      for (int j = 0; j < N - 1; ++j) cr[j] = df_sub(cr[j], df_mul(df_div(cr[j], sum), dif));
     }
   }
-  double p_eq;
-  const unsigned st = relax_face<N>(k, sl, cr, p_eq);
-  // the face record: FP32 state with the critical slots rounded from FP64, the volume
-  // fractions as make_sol limits them, the equilibrium pressure for every material
-  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
-  double at[N], sum = 0.0;
+  float p_eq;
+  const unsigned st = relax_face_df<N>(k, sl, cr, p_eq);
+  // the face record: FP32 state with the critical slots rounded from their pairs, the
+  // volume fractions as make_sol limits them, the equilibrium pressure for every material
+  df at[N];
+  df sum = df_make(0.0f);
 #pragma unroll
   for (int i = 0; i < N - 1; ++i) {
     at[i] = cr[i];
-    if (at[i] <= lo) at[i] = lo;
-    else if (at[i] >= hi) at[i] = hi;
-    sum += at[i];
+    if (df_le(at[i], k.alo_d)) at[i] = k.alo_d;
+    else if (df_le(k.ahi_d, at[i])) at[i] = k.ahi_d;
+    sum = df_add(sum, at[i]);
   }
-  if (sum > hi) {
-    const double dif = sum - hi;
+  if (df_lt(k.ahi_d, sum)) {
+    const df dif = df_sub(sum, k.ahi_d);
 #pragma unroll
-    for (int j = 0; j < N - 1; ++j) at[j] -= (at[j] / sum) * dif;
-    sum = hi;
+    for (int j = 0; j < N - 1; ++j) at[j] = df_sub(at[j], df_mul(df_div(at[j], sum), dif));
+    sum = k.ahi_d;
   }
-  at[N - 1] = 1.0 - sum;
+  at[N - 1] = df_sub(df_make(1.0f), sum);
   float *out = SF + (int64_t)f * RL::SIZE * m.n + c;
 #pragma unroll
-  for (int j = N - 1; j < NCR; j++) sl[crit_slot<N>(j)] = (float)cr[j];
+  for (int j = N - 1; j < NCR; j++) sl[crit_slot<N>(j)] = df_to_float(cr[j]);
 #pragma unroll
-  for (int i = 0; i < N - 1; ++i) sl[C::i3 + i] = (float)at[i];
+  for (int i = 0; i < N - 1; ++i) sl[C::i3 + i] = df_to_float(at[i]);
 #pragma unroll
   for (int i = 0; i < C::NEQ; i++) out[(int64_t)i * m.n] = sl[i];
-  out[(int64_t)RL::AL * m.n] = (float)at[N - 1];
-  const float pf = (float)p_eq;
+  out[(int64_t)RL::AL * m.n] = df_to_float(at[N - 1]);
 #pragma unroll
-  for (int i = 0; i < N; ++i) out[(int64_t)(RL::P + i) * m.n] = pf;
+  for (int i = 0; i < N; ++i) out[(int64_t)(RL::P + i) * m.n] = p_eq;
   if (st) atomicOr(status, st);
 }
 
@@ -1373,14 +1409,18 @@ __global__ void __launch_bounds__(128) m5f_relax_cell(int64_t n, M5Consts k,
 }  // namespace
 
 void ffv_m5f_shadow(int64_t n, const M5Consts &k, const double *S, float *Sf, cudaStream_t st) {
-  m5f_shadow<<<152 * 8, 256, 0, st>>>((int64_t)ffv_m5_neq(k.nmat) * n, S, Sf);
+  float *Sflo = Sf + (int64_t)ffv_m5_neq(k.nmat) * n;
+  if (k.nmat == 2) m5f_shadow<2><<<152 * 8, 256, 0, st>>>(n, S, Sf, Sflo);
+  else m5f_shadow<3><<<152 * 8, 256, 0, st>>>(n, S, Sf, Sflo);
 }
 
 void ffv_m5f_recon(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
                    const float *Sf, float *SFf, unsigned *status, cudaStream_t st) {
+  (void)S;
+  const float *Sflo = Sf + (int64_t)ffv_m5_neq(k.nmat) * m.n;
   const unsigned blocks = (unsigned)((6 * m.n + 127) / 128);
-  if (k.nmat == 2) m5f_recon_face<2><<<blocks, 128, 0, st>>>(m, g, k, S, Sf, SFf, status);
-  else m5f_recon_face<3><<<blocks, 128, 0, st>>>(m, g, k, S, Sf, SFf, status);
+  if (k.nmat == 2) m5f_recon_face<2><<<blocks, 128, 0, st>>>(m, g, k, Sf, Sflo, SFf, status);
+  else m5f_recon_face<3><<<blocks, 128, 0, st>>>(m, g, k, Sf, Sflo, SFf, status);
 }
 
 void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
