@@ -1,24 +1,29 @@
 // Model-5 FP32-flux form: face reconstruction, wave speeds, star states and HLLC /
-// ghost-fluid HLLC fluxes in FP32; FP64 where cancellation needs it.
+// ghost-fluid HLLC fluxes in FP32; double-float (FP32 pairs, ffv_df.cuh) where cancellation
+// needs more than FP32, FP64 only for the RK state and the residual sums.
 //
 // The algorithm is the FP64 form's (ffv_m5_fp64.cu, itself the reference's m5_* code), with
 // these precision choices:
-//   * MUSCL slopes and limiter in FP32.  Face values are formed in FP64 as the cell value
-//     plus the FP32 slope correction, because the stiffened-gas pressure recovery below
-//     divides and cancels the volume fractions and internal energies.
+//   * MUSCL slopes and limiter in FP32 on an FP32 copy of the state.  The "critical" slots
+//     -- volume fractions, internal energies, total energy, which the stiffened-gas
+//     pressure recovery divides and cancels -- are carried as double-float pairs (the low
+//     parts written by m5f_shadow once per cell and stage): their face values are the pair
+//     plus the FP32 slope correction, their slopes the pairs' differences.
 //   * Pressure relaxation of a face or cell state: each material's initial pressure
 //     p_k = (gamma_k - 1)(alpha rho e_k - e_el) / alpha_k - gamma_k p_inf_k (a difference
 //     of two ~1e9 numbers for a liquid with p_inf 6e8, divided by alpha_k that can be
-//     1e-8) and the final energy-consistent equilibrium pressure and internal energies
-//     are FP64; the Newton iteration on the equilibrium pressure in between is FP32 (it
-//     only has to locate the volume fractions, which are then used in FP64).
+//     1e-8) and the final energy-consistent equilibrium pressure and internal energies in
+//     double-float; the Newton iteration on the equilibrium pressure in between in FP32 (it
+//     only has to locate the volume fractions).  GB300 runs FP64 at 1/64 of the FP32 rate,
+//     and FP64<->FP32 conversions share that pipe: double-float keeps this work on the FP32
+//     pipe.
 //   * The face record handed to the flux kernel holds the face state in FP32 plus each
-//     material's pressure recovered in FP64 (rounded once to FP32) and the last
-//     material's volume fraction (1 - sum in FP64: in FP32 that difference would lose a
-//     1e-6 fraction next to 1).
+//     material's recovered pressure (rounded once to FP32) and the last material's volume
+//     fraction (1 - sum formed on the pairs: in FP32 that difference would lose a 1e-6
+//     fraction next to 1).
 //   * Wave speeds, star region, physical flux, HLLC and its ghost-fluid variant: FP32.
 //     Face fluxes are stored as FP32 and summed into the FP64 cell residual by
-//     m5_cell_update; the RK state stays FP64.
+//     m5f_cell_update; the RK state stays FP64.
 // Compiled with FMA contraction (no bit-exactness goal here: the error against the FP64
 // form is measured instead).
 #include <math.h>
@@ -378,210 +383,6 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
   return st;
 }
 
-// ------------------------------------------------------------ relaxation, mixed precision
-template <int N>
-__device__ __forceinline__ void vf_limit_relax_d(const M5Consts &k, double *avf, bool elseif) {
-  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
-  double sum = 0.0;
-#pragma unroll
-  for (int i = 0; i < N - 1; ++i) {
-    if (elseif) {
-      if (avf[i] <= lo) avf[i] = lo;
-      else if (avf[i] >= hi) avf[i] = hi;
-    } else {
-      if (avf[i] <= lo) avf[i] = lo;
-      if (avf[i] >= hi) avf[i] = hi;
-    }
-    sum += avf[i];
-  }
-  if (sum >= hi) {
-    const double dif = sum - hi;
-#pragma unroll
-    for (int j = 0; j < N - 1; ++j) avf[j] = avf[j] - (avf[j] / sum) * dif;
-    sum = hi;
-  }
-  avf[N - 1] = 1.0 - sum;
-}
-
-// m5_relaxationvec.c's PRELAX 1 / 3 on V (FP64 state vector) with the Newton iteration in
-// FP32.  avf_out (optional) receives all N volume fractions and p_out the equilibrium
-// pressure (each material's pressure after relaxation).
-template <int N>
-__device__ unsigned relax_mixed(const M5Consts &k, double *V, double *avf_out, double *p_out) {
-  using C = K5<N>;
-  double ar[N], are[N], avf[N], avf0[N];
-  float A[9], G[9], Gmag;
-  double rho = 0.0;
-#pragma unroll
-  for (int iv = 0; iv < N; ++iv) {
-    ar[iv] = V[iv + C::i0];
-    are[iv] = V[iv + C::i4];
-    rho += ar[iv];
-  }
-  const double irho = 1.0 / rho;
-  const double u = V[C::i1 + 0] * irho, v = V[C::i1 + 1] * irho, w = V[C::i1 + 2] * irho;
-  const double rE = V[C::i2];
-#pragma unroll
-  for (int iv = 0; iv < N - 1; ++iv) avf[iv] = V[iv + C::i3];
-  vf_limit_relax_d<N>(k, avf, true);
-#pragma unroll
-  for (int iv = 0; iv < N; ++iv) avf0[iv] = avf[iv];
-#pragma unroll
-  for (int q = 0; q < 9; q++) A[q] = (float)V[q + C::i5];
-  gmat_f(A, G, Gmag);
-  double ael[N];
-#pragma unroll
-  for (int iv = 0; iv < N; ++iv) ael[iv] = (double)elastic_energy_f(G, Gmag, k.mu_f[iv]);
-  const double eps_sml = 1.0e-12, eps_big = 1.0e-8;
-  unsigned st = 0;
-  double ratio = 1.0;
-  if (k.prelax == 1) {  // closed form for two materials, FP64 (no iteration)
-    double t0[N], p0[N];
-#pragma unroll
-    for (int iv = 0; iv < N; ++iv) {
-      t0[iv] = avf[iv] / ar[iv];
-      p0[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) - k.gamma[iv] * k.pinf[iv];
-    }
-    const double *ga = k.gamma, *pi = k.pinf;
-    const double w0 = avf[0] / ga[0], w1 = avf[1] / ga[1];
-    const double A_1 = w0 * (p0[0] + pi[0]) / (w0 + w1);
-    const double A_2 = w1 * (p0[1] + pi[1]) / (w0 + w1);
-    const double d = (A_2 - A_1 - (pi[1] - pi[0]));
-    const double pe = 0.5 * (A_1 + A_2 - (pi[0] + pi[1])) + sqrt(0.25 * (d * d) + A_1 * A_2);
-    if (isnan(pe)) st |= FFV_ST_NAN;
-#pragma unroll
-    for (int iv = 0; iv < N; ++iv) {
-      const double t1 = t0[iv] * (p0[iv] + ga[iv] * pi[iv] + (ga[iv] - 1.0) * pe) /
-                        (pe + ga[iv] * pi[iv] + (ga[iv] - 1.0) * pe);
-      avf[iv] = ar[iv] * t1;
-    }
-    vf_limit_relax_d<N>(k, avf, false);
-    ratio = avf[0] / avf0[0];
-  } else {  // PRELAX 3
-    double pkinit[N];
-#pragma unroll
-    for (int iv = 0; iv < N; ++iv) {
-      if (avf[iv] < 0.0 || ar[iv] < 0.0) {
-        avf[iv] = eps_sml;
-        ar[iv] = eps_sml;
-        are[iv] = eps_sml;
-      }
-      if (avf[iv] >= 1.0) avf[iv] = 1.0 - eps_sml;
-    }
-    bool irelax = true;
-#pragma unroll
-    for (int iv = 0; iv < N; ++iv)
-      if (avf[iv] > 1.0 - eps_sml) irelax = false;
-    if (irelax) {
-      double p0 = 0.0;
-#pragma unroll
-      for (int iv = 0; iv < N; ++iv) {
-        if (avf[iv] > eps_sml) {
-          // stiffened-gas pressure recovery: FP64
-          pkinit[iv] = ((k.gamma[iv] - 1.0) * (are[iv] - ael[iv]) / avf[iv]) -
-                       k.gamma[iv] * k.pinf[iv];
-          const double floor_p = -(1.0 - eps_big) * k.pinf[iv] + eps_big;
-          if (pkinit[iv] <= floor_p) pkinit[iv] = floor_p;
-        } else {
-          pkinit[iv] = 0.0;
-        }
-        p0 += avf[iv] * pkinit[iv];
-      }
-      // Newton on sum_k alpha_k(p) = 1 along each material's isentrope,
-      // alpha_k(p) = alpha_k0 ((p + pi_k) / (pk_k + pi_k))^(-1/gamma_k), in FP32.  The sum is
-      // formed in delta form, F = (sum_k alpha_k0 - 1) + sum_k alpha_k0 e_k with
-      // e_k = expm1(-log1p(x_k) / gamma_k), x_k = (p - pk_k) / (pk_k + pi_k), so that every
-      // term keeps FP32 precision relative to its own size: summing alpha_k(p) - 1 directly
-      // would resolve a 1e-6 volume fraction next to 1 - 1e-6 only to ~6e-8, which
-      // p_inf = 6e8 turns into ~200 Pa.
-      float a0[N], pkf[N], pif[N], b0[N], ig[N], e[N], plo[N], preset[N];
-      double sum0 = -1.0;
-#pragma unroll
-      for (int iv = 0; iv < N; ++iv) {
-        if (avf[iv] > eps_sml) sum0 += avf[iv];
-        a0[iv] = (float)avf[iv];
-        pkf[iv] = (float)pkinit[iv];
-        pif[iv] = k.pinf_f[iv];
-        b0[iv] = (float)(1.0 / (pkinit[iv] + k.pinf[iv]));
-        ig[iv] = k.igam_f[iv];
-        plo[iv] = k.plo_f[iv];
-        preset[iv] = k.preset_f[iv];
-        e[iv] = 0.0f;
-      }
-      const float F0 = (float)sum0;
-      float pf = (float)p0, F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
-      // the iterate settles within a few steps; the cap bounds the loop
-#pragma unroll 1
-      for (int iter = 0; iter < 64; iter++) {
-        const float step = F / dF;
-        if (iter > 0 && !(fabsf(step) > 1.0e-7f * fabsf(pf))) break;
-        pf = pf - step;
-#pragma unroll
-        for (int iv = 0; iv < N; ++iv)
-          if (pf < plo[iv]) pf = preset[iv];
-        if (pf == prev1 || pf == prev2) break;
-        F = F0;
-        dF = 0.0f;
-#pragma unroll
-        for (int iv = 0; iv < N; ++iv) {
-          if (avf[iv] > eps_sml) {
-            const float x = (pf - pkf[iv]) * b0[iv];
-            // 1 + x = (p + pi) / (pk + pi); near the pressure floor it is formed directly
-            const float opx = x > -0.5f ? 1.0f + x : fmaxf((pf + pif[iv]) * b0[iv], 1.0e-30f);
-            const float lx = x > -0.5f ? log1pf(x) : logf(opx);
-            e[iv] = expm1f(-lx * ig[iv]);
-            F += a0[iv] * e[iv];
-            dF -= a0[iv] * (1.0f + e[iv]) * ig[iv] * b0[iv] / opx;
-          }
-        }
-        if (isnan(pf) || isnan(F) || isnan(dF)) {
-          st |= FFV_ST_NAN;
-          break;
-        }
-        prev2 = prev1;
-        prev1 = pf;
-      }
-#pragma unroll
-      for (int iv = 0; iv < N; ++iv)
-        if (avf[iv] > eps_sml) avf[iv] = avf[iv] + avf[iv] * (double)e[iv];
-      vf_limit_relax_d<N>(k, avf, true);
-    }
-    const int i_as = ((avf[0] < avf[1]) && (k.mu[1] != 0.0)) ? 1 : 0;
-    ratio = avf[i_as] / avf0[i_as];
-  }
-  // energy-consistent equilibrium pressure and internal energies: FP64
-  double e_elast = 0.0;
-#pragma unroll
-  for (int iv = 0; iv < N; ++iv) e_elast += ael[iv] * irho;
-  const double e_hyd = rE * irho - 0.5 * (u * u + v * v + w * w) - e_elast;
-  double num = 0.0, den = 0.0;
-#pragma unroll
-  for (int iv = 0; iv < N; ++iv) {
-    const double ig1 = 1.0 / (k.gamma[iv] - 1.0);
-    num += avf[iv] * (k.gamma[iv] * k.pinf[iv] * ig1);
-    den += avf[iv] * ig1;
-  }
-  const double p_relaxed = (rho * e_hyd - num) / den;
-#pragma unroll
-  for (int iv = 0; iv < N - 1; ++iv) {
-    if (isnan(avf[iv])) st |= FFV_ST_NAN;
-    V[iv + C::i3] = avf[iv];
-  }
-#pragma unroll
-  for (int iv = 0; iv < N; iv++) {
-    const double a2 = avf[iv] * (p_relaxed + k.gamma[iv] * k.pinf[iv]) / (k.gamma[iv] - 1.0) + ael[iv];
-    if (isnan(a2)) st |= FFV_ST_NAN;
-    V[iv + C::i4] = a2;
-  }
-#pragma unroll
-  for (int q = 0; q < 9; ++q) V[q + C::i5] = V[q + C::i5] * ratio;
-  if (avf_out)
-#pragma unroll
-    for (int iv = 0; iv < N; ++iv) avf_out[iv] = avf[iv];
-  if (p_out) *p_out = p_relaxed;
-  return st;
-}
-
 // avf_limit.c:3-21 on a state vector
 template <int N>
 __device__ __forceinline__ void avf_limit_d(const M5Consts &k, double *S) {
@@ -805,10 +606,11 @@ __device__ __forceinline__ void vf_limit_relax_df(const M5Consts &k, df *avf, bo
 
 // m5_relaxationvec.c on a face state: FP32 partial densities, momentum and deformation in
 // v, the critical slots in cr as double-float pairs; the pressure recovery and the
-// energy-consistent equilibrium in double-float, the Newton iteration as relax_mixed's in
-// FP32.  PRELAX 1 (the two-material closed form) converts to FP64 and back.
+// energy-consistent equilibrium in double-float, the Newton iteration in FP32 (below).
+// PRELAX 1 (the two-material closed form) converts to FP64 and back.
 template <int N>
-__device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_out) {
+__device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_out,
+                                  df *ratio_out = nullptr) {
   using C = K5<N>;
   df ar[N], are[N], avf[N], avf0[N];
   float ael[N];
@@ -832,7 +634,7 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
 #pragma unroll
   for (int iv = 0; iv < N; ++iv) ael[iv] = elastic_energy_f(G, Gmag, k.mu_f[iv]);
   unsigned st = 0;
-  float ratio = 1.0f;
+  df ratio = df_make(1.0f);
   if (k.prelax == 1) {  // closed form for two materials, in FP64
     double a[N], t0[N], p0[N];
 #pragma unroll
@@ -854,7 +656,7 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
       avf[iv] = df_from_double((double)ar[iv].hi * t0[iv] * (p0[iv] + k.gpi[iv] + (ga[iv] - 1.0) * pe) /
                                (pe + k.gpi[iv] + (ga[iv] - 1.0) * pe));
     vf_limit_relax_df<N>(k, avf, false);
-    ratio = df_to_float(avf[0]) / df_to_float(avf0[0]);
+    ratio = df_div(avf[0], avf0[0]);
   } else {  // PRELAX 3
 #pragma unroll
     for (int iv = 0; iv < N; ++iv) {
@@ -894,6 +696,14 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
         preset[iv] = k.preset_f[iv];
         e[iv] = 0.0f;
       }
+      // Newton on sum_k alpha_k(p) = 1 along each material's isentrope,
+      // alpha_k(p) = alpha_k0 ((p + pi_k) / (pk_k + pi_k))^(-1/gamma_k), in FP32.  The sum
+      // is formed in delta form, F = (sum_k alpha_k0 - 1) + sum_k alpha_k0 e_k with
+      // e_k = expm1(-log1p(x_k) / gamma_k), x_k = (p - pk_k) / (pk_k + pi_k), so that every
+      // term keeps FP32 precision relative to its own size: summing alpha_k(p) - 1 directly
+      // would resolve a 1e-6 volume fraction next to 1 - 1e-6 only to ~6e-8, which
+      // p_inf = 6e8 turns into ~200 Pa.  The iterate settles within a few steps; the cap
+      // bounds the loop.
       const float F0 = df_to_float(sum0);
       float pf = df_to_float(p0), F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
 #pragma unroll 1
@@ -931,7 +741,7 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
       vf_limit_relax_df<N>(k, avf, true);
     }
     const int i_as = (df_lt(avf[0], avf[1]) && (k.mu[1] != 0.0)) ? 1 : 0;
-    ratio = df_to_float(avf[i_as]) / df_to_float(avf0[i_as]);
+    ratio = df_div(avf[i_as], avf0[i_as]);
   }
   df num = df_make(0.0f), den = df_make(0.0f);
   float sael = 0.0f;
@@ -953,9 +763,43 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
     if (df_isnan(a2)) st |= FFV_ST_NAN;
     cr[N - 1 + iv] = a2;
   }
+  const float rf32 = df_to_float(ratio);
 #pragma unroll
-  for (int q = 0; q < 9; ++q) v[C::i5 + q] *= ratio;
+  for (int q = 0; q < 9; ++q) v[C::i5 + q] *= rf32;
   p_out = df_to_float(p);
+  if (ratio_out) *ratio_out = ratio;
+  return st;
+}
+
+// m5_relaxationvec.c's PRELAX 1 / 3 on an FP64 cell state V: the values it reads converted
+// once to double-float pairs, the pressure recovery and the energy-consistent equilibrium
+// in double-float, the Newton iteration in FP32 (as relax_face_df), the results converted
+// back to FP64.
+template <int N>
+__device__ unsigned relax_cell_df(const M5Consts &k, double *V) {
+  using C = K5<N>;
+  // relax_face_df's inputs: the FP32 partial densities, momentum and deformation, and the
+  // critical slots as pairs
+  float v[C::NEQ];
+#pragma unroll
+  for (int i = 0; i < C::NEQ; i++) v[i] = (float)V[i];
+  df cr[2 * N];
+#pragma unroll
+  for (int j = 0; j < 2 * N; j++) cr[j] = df_from_double(V[crit_slot<N>(j)]);
+  // relax_face_df takes the kinetic energy from FP32 momentum and partial densities; for a
+  // cell the partial densities enter the Newton iteration and the recovery as FP32 values,
+  // their sum is the density of the kinetic energy
+  float p_eq;
+  df ratio;
+  const unsigned st = relax_face_df<N>(k, v, cr, p_eq, &ratio);
+#pragma unroll
+  for (int iv = 0; iv < N - 1; ++iv) V[C::i3 + iv] = (double)cr[iv].hi + (double)cr[iv].lo;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv)
+    V[C::i4 + iv] = (double)cr[N - 1 + iv].hi + (double)cr[N - 1 + iv].lo;
+  const double r = (double)ratio.hi + (double)ratio.lo;
+#pragma unroll
+  for (int q = 0; q < 9; ++q) V[C::i5 + q] = V[C::i5 + q] * r;
   return st;
 }
 
@@ -1398,7 +1242,7 @@ __global__ void __launch_bounds__(128) m5f_relax_cell(int64_t n, M5Consts k,
   double s[C::NEQ];
   load_state<N>(Sin, n, c, s);
   const double phi_old = s[C::i3] - k.avf_lim;
-  const unsigned st = relax_mixed<N>(k, s, nullptr, nullptr);
+  const unsigned st = relax_cell_df<N>(k, s);
   const double phi_new = (k.mu[0] != 0.0) ? s[C::i3] - k.avf_lim : phi_old;
   flag[c] = (phi_old * phi_new < 0.0) ? 1 : 0;
 #pragma unroll
