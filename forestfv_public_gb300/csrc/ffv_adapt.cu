@@ -64,54 +64,82 @@ extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *spl
   int rc = ffv_ctx_adapt_view(ctx, &device, &st, &n, &neq, &d_S, &model, &k);
   if (rc != FFV_OK) return rc;
   if (n != m->n) return FFV_ERR_ARG;
-  std::vector<int32_t> tij, lev, cij;
-  std::vector<int64_t> map;
-  tij.reserve(3 * n);
-  lev.reserve(n);
-  cij.reserve(3 * n);
-  map.reserve(n);
+  // what becomes of each old leaf: 8 split (eight leaves out), 1 kept, 2 the first of a
+  // merging group (its parent out), 0 the other seven of a merging group; then a prefix
+  // sum and the new leaf list written in parallel, in the order one sweep in leaf order
+  // gives
+  const int nth = host_threads();
+  std::vector<uint8_t> cnt(n);
+  std::vector<int64_t> tsum(nth + 1, 0), tmerged(nth, 0);
+  int bad = 0;
+  parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
+    int64_t acc = 0;
+    for (int64_t c = a; c < b; c++) {
+      const int l = ffv_info_level(m->info[c]);
+      const int64_t g = l > 1 ? ffv_sibling_group(m, c) : -1;
+      bool merge = g >= 0;
+      for (int q = 0; q < 8 && merge; q++) merge = split[g + q] < l;
+      uint8_t k;
+      if (merge) k = (g == c) ? 2 : 0;
+      else if (split[c] > l) k = 8;
+      else k = 1;
+      if (k == 8 && l + 1 > FFV_MAX_LEVEL) __atomic_store_n(&bad, 1, __ATOMIC_RELAXED);
+      if (k == 2) tmerged[t]++;
+      cnt[c] = k;
+      acc += k == 2 ? 1 : k;
+    }
+    tsum[t + 1] = acc;
+  });
+  if (bad) return FFV_ERR_TABLE;
+  for (int t = 0; t < nth; t++) tsum[t + 1] += tsum[t];
+  const int64_t n_out = tsum[nth];
   int64_t nmerged = 0;
-  for (int64_t c = 0; c < n;) {
-    const int l = ffv_info_level(m->info[c]);
-    const int32_t *t = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
-    if (l > 1 && ffv_sibling_group(m, c) == c) {
-      {
-        bool all = true;
-        for (int q = 0; q < 8 && all; q++) all = split[c + q] < l;
-        if (all) {  // merge.c: the parent of eight leaves
-          tij.insert(tij.end(), {t[0], t[1], t[2]});
-          lev.push_back(l - 1);
-          cij.insert(cij.end(), {x[0] >> 1, x[1] >> 1, x[2] >> 1});
-          map.push_back(-1 - c);
-          nmerged++;
-          c += 8;
-          continue;
+  for (int t = 0; t < nth; t++) nmerged += tmerged[t];
+  std::vector<int32_t> tij(3 * n_out), lev(n_out), cij(3 * n_out);
+  std::vector<int64_t> map(n_out);
+  parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
+    int64_t o = tsum[t];
+    for (int64_t c = a; c < b; c++) {
+      if (cnt[c] == 0) continue;
+      const int l = ffv_info_level(m->info[c]);
+      const int32_t *tr = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
+      if (cnt[c] == 2) {  // merge.c: the parent of eight leaves
+        for (int d = 0; d < 3; d++) {
+          tij[3 * o + d] = tr[d];
+          cij[3 * o + d] = x[d] >> 1;
         }
+        lev[o] = l - 1;
+        map[o] = -1 - c;
+        o++;
+      } else if (cnt[c] == 8) {  // split.c: eight children in child order, corner k at (bit1, bit0, bit2)
+        for (int q = 0; q < 8; q++, o++) {
+          for (int d = 0; d < 3; d++) tij[3 * o + d] = tr[d];
+          cij[3 * o] = 2 * x[0] + ((q >> 1) & 1);
+          cij[3 * o + 1] = 2 * x[1] + (q & 1);
+          cij[3 * o + 2] = 2 * x[2] + ((q >> 2) & 1);
+          lev[o] = l + 1;
+          map[o] = c;
+        }
+      } else {
+        for (int d = 0; d < 3; d++) {
+          tij[3 * o + d] = tr[d];
+          cij[3 * o + d] = x[d];
+        }
+        lev[o] = l;
+        map[o] = c;
+        o++;
       }
     }
-    if (split[c] > l) {  // split.c: eight children in child order, corner k at (bit1, bit0, bit2)
-      if (l + 1 > FFV_MAX_LEVEL) return FFV_ERR_TABLE;
-      for (int q = 0; q < 8; q++) {
-        tij.insert(tij.end(), {t[0], t[1], t[2]});
-        lev.push_back(l + 1);
-        cij.insert(cij.end(), {2 * x[0] + ((q >> 1) & 1), 2 * x[1] + (q & 1), 2 * x[2] + ((q >> 2) & 1)});
-        map.push_back(c);
-      }
-    } else {
-      tij.insert(tij.end(), {t[0], t[1], t[2]});
-      lev.push_back(l);
-      cij.insert(cij.end(), {x[0], x[1], x[2]});
-      map.push_back(c);
-    }
-    c++;
-  }
+  });
   const int64_t n_new = (int64_t)lev.size();
   ffv_mesh *nm = nullptr;
   std::vector<int64_t> order(n_new);
   rc = ffv_mesh_build(&m->desc, n_new, tij.data(), lev.data(), cij.data(), &nm, order.data());
   if (rc != FFV_OK) return rc;
   std::vector<int64_t> cmap(n_new);
-  for (int64_t j = 0; j < n_new; j++) cmap[j] = map[order[j]];
+  parallel_chunks(n_new, nth, [&](int, int64_t a, int64_t b) {
+    for (int64_t j = a; j < b; j++) cmap[j] = map[order[j]];
+  });
   if (src) memcpy(src, cmap.data(), sizeof(int64_t) * n_new);
   // carry the state over on the device, then swap the tables
   cudaError_t e = cudaSetDevice(device);

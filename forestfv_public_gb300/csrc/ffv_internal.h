@@ -55,6 +55,28 @@ struct ffv_level_geom {
 struct ffv_mesh;
 int64_t ffv_sibling_group(const ffv_mesh *m, int64_t c);
 
+#ifdef __cplusplus
+#include <algorithm>
+#include <thread>
+#include <vector>
+
+// fn(thread, begin, end) on nthreads contiguous chunks of [0, n), the calling thread taking
+// the first
+template <typename Fn>
+inline void parallel_chunks(int64_t n, int nthreads, Fn fn) {
+  const int64_t chunk = (n + nthreads - 1) / nthreads;
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; t++)
+    pool.emplace_back([&, t] { fn(t, std::min(n, t * chunk), std::min(n, (t + 1) * chunk)); });
+  fn(0, 0, std::min(n, chunk));
+  for (auto &th : pool) th.join();
+}
+
+inline int host_threads() {
+  return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+}
+#endif
+
 struct ffv_mesh {
   ffv_forest_desc desc;
   int64_t n;

@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <new>
 #include <thread>
 #include <vector>
@@ -123,34 +124,24 @@ uint64_t cell_key(int level, uint32_t gx, uint32_t gy, uint32_t gz) {
 }
 
 // fn(t, c0, c1) over [0, n) in nthreads contiguous chunks, on nthreads host threads
-template <typename Fn>
-void parallel_chunks(int64_t n, int nthreads, Fn fn) {
-  const int64_t chunk = (n + nthreads - 1) / nthreads;
-  std::vector<std::thread> pool;
-  for (int t = 1; t < nthreads; t++)
-    pool.emplace_back([&, t] { fn(t, std::min(n, t * chunk), std::min(n, (t + 1) * chunk)); });
-  fn(0, 0, std::min(n, chunk));
-  for (auto &th : pool) th.join();
-}
-
-int host_threads() {
-  return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
-}
-
 // open-addressing map from cell keys to cell indices (linear probing, power-of-two size;
 // filled once, then only read -- from several threads)
 struct CellMap {
-  std::vector<uint64_t> keys;
-  std::vector<int32_t> vals;  // -1: empty slot
+  // key and value side by side: a probe touches one cache line
+  struct Slot {
+    uint64_t key;
+    int32_t val;  // -1: empty slot
+    int32_t pad;
+  };
+  std::unique_ptr<Slot[]> slot;  // allocated without initialisation, filled in parallel
   uint64_t mask = 0;
   CellMap(int64_t n, int nthreads) {
     uint64_t cap = 16;
     while (cap < (uint64_t)(2 * n)) cap <<= 1;
-    keys.resize(cap);
-    vals.resize(cap);
+    slot.reset(new Slot[cap]);
     mask = cap - 1;
     parallel_chunks((int64_t)cap, nthreads, [&](int, int64_t a, int64_t b) {
-      for (int64_t i = a; i < b; i++) vals[i] = -1;
+      for (int64_t i = a; i < b; i++) slot[i].val = -1;
     });
   }
   static uint64_t mix(uint64_t z) {
@@ -164,17 +155,18 @@ struct CellMap {
   void put_new(uint64_t k, int32_t v) {
     for (uint64_t i = mix(k) & mask;; i = (i + 1) & mask) {
       int32_t expect = -1;
-      if (__atomic_compare_exchange_n(&vals[i], &expect, v, false, __ATOMIC_RELAXED,
+      if (__atomic_compare_exchange_n(&slot[i].val, &expect, v, false, __ATOMIC_RELAXED,
                                       __ATOMIC_RELAXED)) {
-        keys[i] = k;
+        slot[i].key = k;
         return;
       }
     }
   }
   int32_t get(uint64_t k) const {
     for (uint64_t i = mix(k) & mask;; i = (i + 1) & mask) {
-      if (vals[i] < 0) return -1;
-      if (keys[i] == k) return vals[i];
+      const Slot &e = slot[i];
+      if (e.val < 0) return -1;
+      if (e.key == k) return e.val;
     }
   }
 };
@@ -241,16 +233,24 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
     if (lkey[a] != lkey[b]) return lkey[a] < lkey[b];
     return level[a] < level[b];
   };
-  bool sorted = true;  // leaves given in canonical order (a regrid's output) need no sort
-  for (int64_t i = 0; i + 1 < nleaves && sorted; i++) sorted = !before(i + 1, i);
-  if (!sorted) std::sort(perm.begin(), perm.end(), before);
+  // leaves given in canonical order (a regrid's output) need no sort
+  std::vector<char> unsorted(nthreads, 0), overlap(nthreads, 0);
+  parallel_chunks(nleaves > 0 ? nleaves - 1 : 0, nthreads, [&](int t, int64_t a, int64_t b) {
+    for (int64_t i = a; i < b && !unsorted[t]; i++) unsorted[t] = before(i + 1, i);
+  });
+  if (std::any_of(unsorted.begin(), unsorted.end(), [](char x) { return x != 0; }))
+    std::sort(perm.begin(), perm.end(), before);
   // overlap check: a leaf's key range must end before the next leaf of the same tree starts
-  for (int64_t k = 0; k + 1 < nleaves; k++) {
-    int64_t a = perm[k], b = perm[k + 1];
-    if (tkey[a] != tkey[b]) continue;
-    uint64_t span = 1ULL << (3 * (D - (level[a] - 1)));
-    if (lkey[a] + span > lkey[b]) return FFV_ERR_TABLE;
-  }
+  parallel_chunks(nleaves > 0 ? nleaves - 1 : 0, nthreads, [&](int t, int64_t c0, int64_t c1) {
+    for (int64_t k = c0; k < c1 && !overlap[t]; k++) {
+      int64_t a = perm[k], b = perm[k + 1];
+      if (tkey[a] != tkey[b]) continue;
+      uint64_t span = 1ULL << (3 * (D - (level[a] - 1)));
+      if (lkey[a] + span > lkey[b]) overlap[t] = 1;
+    }
+  });
+  if (std::any_of(overlap.begin(), overlap.end(), [](char x) { return x != 0; }))
+    return FFV_ERR_TABLE;
 
   ffv_mesh *m = new (std::nothrow) ffv_mesh();
   if (!m) return FFV_ERR_NOMEM;
@@ -332,21 +332,45 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
   // afterwards, which gives the numbering of one sweep in cell order
   std::vector<std::vector<int32_t>> csub(nthreads);
   std::vector<int> crc(nthreads, FFV_OK);
+  // first cell of c's complete group of eight sibling leaves (consecutive in canonical
+  // order, child indices 0..7, one parent), or -1: a face between two of them needs no
+  // lookup, the neighbour is the sibling with that axis' bit flipped
+  auto kid_of = [&](int64_t c) {
+    return (int)(((gx[3 * c] & 1) << 1) | (gx[3 * c + 1] & 1) | ((gx[3 * c + 2] & 1) << 2));
+  };
+  auto group_start = [&](int64_t c, int l) -> int64_t {
+    if (l <= 1) return -1;
+    const int64_t s0 = c - kid_of(c);
+    if (s0 < 0 || s0 + 8 > nleaves) return -1;
+    for (int q = 0; q < 8; q++) {
+      const int64_t o = s0 + q;
+      if (level[perm[o]] != l || kid_of(o) != q) return -1;
+      for (int b = 0; b < 3; b++)
+        if ((gx[3 * o + b] >> 1) != (gx[3 * c + b] >> 1)) return -1;
+    }
+    return s0;
+  };
   auto work = [&](int t) {
     const int64_t c0 = t * chunk, c1 = std::min<int64_t>(nleaves, c0 + chunk);
     std::vector<int32_t> &sub = csub[t];
     for (int64_t c = c0; c < c1; c++) {
       int l = level[perm[c]];
       uint32_t info = (uint32_t)l << 24;
+      const int64_t gs = group_start(c, l);
+      const int kid = kid_of(c);
       for (int f = 0; f < 6; f++) {
         const ffv_face_frame &fr = m->frame[f];
         int a = fr.side_axis;
         int64_t g[3] = {gx[3 * c], gx[3 * c + 1], gx[3 * c + 2]};
+        const int bit = (int)(g[a] & 1);
         g[a] += fr.side_dir;
         int64_t ext = (int64_t)T[a] << (l - 1);
         uint32_t kind;
         int32_t slot = -1;
-        if (g[a] < 0 || g[a] >= ext) {
+        if (gs >= 0 && bit == (fr.side_dir > 0 ? 0 : 1)) {
+          kind = FFV_FK_SAME;  // the sibling across the parent's inner face
+          slot = (int32_t)(gs + (kid ^ (a == 0 ? 2 : (a == 1 ? 1 : 4))));
+        } else if (g[a] < 0 || g[a] >= ext) {
           int side = 2 * a + (fr.side_dir > 0 ? 1 : 0);
           kind = FFV_FK_BC | (uint32_t)desc->bc[side];
         } else {

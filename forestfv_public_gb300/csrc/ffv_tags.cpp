@@ -16,49 +16,77 @@
 extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *split) {
   if (!m || !split || level_max < 0) return FFV_ERR_ARG;
   const int64_t n = m->n;
+  const int nth = host_threads();
   // complete groups of eight sibling leaves (first cell, or -1)
   std::vector<int64_t> group(n);
-  for (int64_t c = 0; c < n; c++) group[c] = ffv_sibling_group(m, c);
+  parallel_chunks(n, nth, [&](int, int64_t a, int64_t b) {
+    for (int64_t c = a; c < b; c++) group[c] = ffv_sibling_group(m, c);
+  });
   auto level = [&](int64_t c) { return (int32_t)ffv_info_level(m->info[c]); };
+  // criterionsmth.c:14-33: a leaf coarsens only with all eight siblings, refines by one
+  auto rule1 = [&](int64_t c) {
+    const int32_t l = level(c);
+    int32_t v = split[c];
+    if (l > 1) {
+      // only leaf children count (criterionsmth.c:19-21): a group with a refined sibling
+      // cannot reach eight
+      const int64_t g = group[c];
+      int imerge = 0;
+      if (g >= 0)
+        for (int64_t q = g; q < g + 8; q++)
+          if (split[q] < level(q)) imerge++;
+      if (imerge == 8) v = l - 1;
+      else if (l > v) v = l;
+    }
+    if (l < v) v = l + 1;
+    return v;
+  };
+  // criterionsmth.c:37-51: at most one level below any face neighbour
+  auto rule2 = [&](int64_t c) {
+    int32_t mx = 1;
+    const uint32_t info = m->info[c];
+    for (int f = 0; f < 6; f++) {
+      const uint32_t kind = ffv_face_kind(info, f);
+      if (kind & FFV_FK_BC) continue;
+      const int32_t s = m->nbr[6 * c + f];
+      if (kind == FFV_FK_FINER) {
+        for (int q = 0; q < 4; q++) mx = std::max(split[m->sub[4 * (int64_t)s + q]], mx);
+      } else {
+        mx = std::max(split[s], mx);
+      }
+    }
+    return mx - split[c] > 1 ? mx - 1 : split[c];
+  };
+  // A sweep updates split in place in leaf order, each leaf seeing its predecessors' new
+  // values.  If no leaf would change when every leaf is evaluated on the values before the
+  // sweep, the in-place sweep changes nothing either (each leaf then sees exactly those
+  // values): that test runs on all host threads and skips the sequential sweep.
+  auto would_change = [&](auto rule) {
+    std::vector<char> hit(nth, 0);
+    parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
+      for (int64_t c = a; c < b && !hit[t]; c++)
+        if (rule(c) != split[c]) hit[t] = 1;
+    });
+    for (char h : hit)
+      if (h) return true;
+    return false;
+  };
   // A pass is a function of `split` alone: once one changes nothing, every later pass
   // would see the same input and change nothing either, so the passes end there.
   for (int32_t pass = 0; pass < level_max + 1; pass++) {
     bool changed = false;
-    // criterionsmth.c:14-33: a leaf coarsens only with all eight siblings, refines by one
-    for (int64_t c = 0; c < n; c++) {
-      const int32_t l = level(c);
-      const int32_t before = split[c];
-      if (l > 1) {
-        // only leaf children count (criterionsmth.c:19-21): a group with a refined sibling
-        // cannot reach eight
-        const int64_t g = group[c];
-        int imerge = 0;
-        if (g >= 0)
-          for (int64_t q = g; q < g + 8; q++)
-            if (split[q] < level(q)) imerge++;
-        if (imerge == 8) split[c] = l - 1;
-        else if (l > split[c]) split[c] = l;
+    if (would_change(rule1)) {
+      for (int64_t c = 0; c < n; c++) {
+        const int32_t v = rule1(c);
+        changed |= v != split[c];
+        split[c] = v;
       }
-      if (l < split[c]) split[c] = l + 1;
-      changed |= split[c] != before;
     }
-    // criterionsmth.c:37-51: at most one level below any face neighbour
-    for (int64_t c = 0; c < n; c++) {
-      int32_t mx = 1;
-      const uint32_t info = m->info[c];
-      for (int f = 0; f < 6; f++) {
-        const uint32_t kind = ffv_face_kind(info, f);
-        if (kind & FFV_FK_BC) continue;
-        const int32_t s = m->nbr[6 * c + f];
-        if (kind == FFV_FK_FINER) {
-          for (int q = 0; q < 4; q++) mx = std::max(split[m->sub[4 * (int64_t)s + q]], mx);
-        } else {
-          mx = std::max(split[s], mx);
-        }
-      }
-      if (mx - split[c] > 1) {
-        split[c] = mx - 1;
-        changed = true;
+    if (would_change(rule2)) {
+      for (int64_t c = 0; c < n; c++) {
+        const int32_t v = rule2(c);
+        changed |= v != split[c];
+        split[c] = v;
       }
     }
     if (!changed) break;
@@ -71,17 +99,24 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
 extern "C" int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit,
                                  int64_t *nmerge) {
   if (!m || !split || !nsplit || !nmerge) return FFV_ERR_ARG;
-  int64_t ns = 0, nm = 0;
-  for (int64_t c = 0; c < m->n; c++) {
-    const int32_t l = (int32_t)ffv_info_level(m->info[c]);
-    if (split[c] > l) ns++;
-    if (l > 1 && ffv_sibling_group(m, c) == c) {
-      bool all = true;
-      for (int q = 0; q < 8 && all; q++) all = split[c + q] < l;
-      nm += all ? 1 : 0;
+  const int nth = host_threads();
+  std::vector<int64_t> ns(nth, 0), nm(nth, 0);
+  parallel_chunks(m->n, nth, [&](int t, int64_t a, int64_t b) {
+    for (int64_t c = a; c < b; c++) {
+      const int32_t l = (int32_t)ffv_info_level(m->info[c]);
+      if (split[c] > l) ns[t]++;
+      if (l > 1 && ffv_sibling_group(m, c) == c) {
+        bool all = true;
+        for (int q = 0; q < 8 && all; q++) all = split[c + q] < l;
+        nm[t] += all ? 1 : 0;
+      }
     }
+  });
+  *nsplit = 0;
+  *nmerge = 0;
+  for (int t = 0; t < nth; t++) {
+    *nsplit += ns[t];
+    *nmerge += nm[t];
   }
-  *nsplit = ns;
-  *nmerge = nm;
   return FFV_OK;
 }
