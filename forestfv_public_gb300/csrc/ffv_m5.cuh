@@ -52,9 +52,10 @@ int ffv_m5_launches_per_stage(const M5Consts &k, int irk);
 void ffv_m5f_shadow(int64_t n, const M5Consts &k, const double *S, float *Sf, cudaStream_t st);
 void ffv_m5f_recon(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
                    const float *Sf, float *SFf, unsigned *status, cudaStream_t st);
+// Sf: the FP32 copy of the state (order 2), or nullptr (order 1: phi0 from S)
 void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
-                  const float *SFf, float *FFf, float *UFf, double *GF, unsigned *status,
-                  cudaStream_t st);
+                  const float *Sf, const float *SFf, float *FFf, float *UFf, double *GF,
+                  unsigned *status, cudaStream_t st);
 // residual + RK stage of the FP32-flux form (the face fluxes of all but the deformation
 // summed in FP64)
 void ffv_m5f_cell_update(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,

@@ -103,7 +103,7 @@ __device__ __forceinline__ void eos_stress_f(float st[3][3], float avf, float pr
 template <int N>
 struct SolF {
   float r, u, v, w, e, ut, vt, wt, c2;
-  double phi0;
+  float phi0;
   float ra[N], avf[N], are[N], p[N];
   float A[9], st[3][3];
   float vec[K5<N>::NC];
@@ -111,7 +111,7 @@ struct SolF {
 
 // primitive state of a face record (m5_facercnstr.c:3-191 with the pressures given)
 template <int N>
-__device__ void make_sol_f(const M5Consts &k, const float *U, double phi0, SolF<N> &s) {
+__device__ void make_sol_f(const M5Consts &k, const float *U, float phi0, SolF<N> &s) {
   using C = K5<N>;
   using RL = RecL<N>;
   s.r = 0.0f;
@@ -173,6 +173,26 @@ __device__ __forceinline__ double cell_phi0(const M5Consts &k, const double *__r
   return ac[0] - k.avf_lim;
 }
 
+// the same from the FP32 copy of the state (order 2: the reconstruction made it); only the
+// sign of phi0 is used (which side of AVF_LIM a cell is on)
+template <int N>
+__device__ __forceinline__ float cell_phi0_f(const M5Consts &k, const float *__restrict__ Sf,
+                                             int64_t n, int64_t c) {
+  using C = K5<N>;
+  float ac[N > 2 ? 2 : 1];
+#pragma unroll
+  for (int i = 0; i < (N > 2 ? 2 : 1); ++i) {
+    float a = Sf[(int64_t)(C::i3 + i) * n + c];
+    if (a >= k.ahi_f) a = k.ahi_f;
+    else if (a <= k.alo_f) a = k.alo_f;
+    ac[i] = a;
+  }
+  const float lim = (float)k.avf_lim;
+  if (N > 2 && k.nsolids == 2 && k.mu[0] != 0.0)
+    return ((ac[0] > ac[N > 2 ? 1 : 0]) ? ac[0] : ac[N > 2 ? 1 : 0]) - lim;
+  return ac[0] - lim;
+}
+
 template <int F, int N>
 __device__ __forceinline__ void ghost_f(const SolF<N> &L, int bc, SolF<N> &R) {
   R = L;
@@ -215,7 +235,7 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
   const float iden = 1.0f / (mR - mL);
   const float s11_S = (mR * sL[0] - mL * sR[0] + mL * mR * (uR - uL)) * iden;
   float s12_S = 0.0f, s13_S = 0.0f;
-  if ((L.phi0 > 0.0) && (R.phi0 > 0.0)) {
+  if ((L.phi0 > 0.0f) && (R.phi0 > 0.0f)) {
     s12_S = (mR * sL[1] - mL * sR[1] + mL * mR * (vR - vL)) * iden;
     s13_S = (mR * sL[2] - mL * sR[2] + mL * mR * (wR - wL)) * iden;
   }
@@ -955,9 +975,9 @@ __device__ __forceinline__ void record_of_cell(const M5Consts &k, const double *
 
 template <int N, int F>
 __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
-                            const double *__restrict__ S, const float *__restrict__ SF, int64_t c,
-                            uint32_t info, float *ff, float uf[3], double &gfm_face, unsigned &st,
-                            bool &owner) {
+                            const double *__restrict__ S, const float *__restrict__ Sf,
+                            const float *__restrict__ SF, int64_t c, uint32_t info, float *ff,
+                            float uf[3], double &gfm_face, unsigned &st, bool &owner) {
   using C = K5<N>;
   using RL = RecL<N>;
   constexpr int FO = fr_opp(F);
@@ -975,11 +995,11 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
   SolF<N> L, R;
   if (k.order == 2) load_record<N>(SF, m.n, F, c, U);
   else record_of_cell<N>(k, S, m.n, c, U);
-  make_sol_f<N>(k, U, cell_phi0<N>(k, S, m.n, c), L);
+  make_sol_f<N>(k, U, Sf ? cell_phi0_f<N>(k, Sf, m.n, c) : (float)cell_phi0<N>(k, S, m.n, c), L);
   if (kind & FFV_FK_BC) {
     const int bc = (int)(kind & 7u);
     ghost_f<F, N>(L, bc, R);
-    const bool gfm = L.phi0 * R.phi0 < 0.0;
+    const bool gfm = L.phi0 * R.phi0 < 0.0f;
     if (gfm) gfm_face = 1.0;
     st |= hllc_acc_f<F, N>(k, L, R, bc, gfm, (float)g.area[l], ff, uf);
     return;
@@ -992,8 +1012,8 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
     const int64_t o = sg ? sg[q] : m.nbr[(int64_t)F * m.n + c];
     if (k.order == 2) load_record<N>(SF, m.n, FO, o, U);
     else record_of_cell<N>(k, S, m.n, o, U);
-    make_sol_f<N>(k, U, cell_phi0<N>(k, S, m.n, o), R);
-    const bool gfm = L.phi0 * R.phi0 < 0.0;
+    make_sol_f<N>(k, U, Sf ? cell_phi0_f<N>(k, Sf, m.n, o) : (float)cell_phi0<N>(k, S, m.n, o), R);
+    const bool gfm = L.phi0 * R.phi0 < 0.0f;
     if (gfm) gfm_face = 1.0;
     float un[3];
     st |= hllc_acc_f<F, N>(k, L, R, 0, gfm, A, ff, un);
@@ -1007,6 +1027,7 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
 template <int N>
 __global__ void __launch_bounds__(128) m5f_face_flux(ffv_dmesh m, ffv_geom g, M5Consts k,
                                                      const double *__restrict__ S,
+                                                     const float *__restrict__ Sf,
                                                      const float *__restrict__ SF,
                                                      float *__restrict__ FF,
                                                      float *__restrict__ UF,
@@ -1023,12 +1044,12 @@ __global__ void __launch_bounds__(128) m5f_face_flux(ffv_dmesh m, ffv_geom g, M5
   unsigned st = 0;
   bool owner = true;
   switch (f) {
-    case 0: face_flux_f<N, 0>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
-    case 1: face_flux_f<N, 1>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
-    case 2: face_flux_f<N, 2>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
-    case 3: face_flux_f<N, 3>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
-    case 4: face_flux_f<N, 4>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
-    default: face_flux_f<N, 5>(m, g, k, S, SF, c, info, ff, uf, gf, st, owner); break;
+    case 0: face_flux_f<N, 0>(m, g, k, S, Sf, SF, c, info, ff, uf, gf, st, owner); break;
+    case 1: face_flux_f<N, 1>(m, g, k, S, Sf, SF, c, info, ff, uf, gf, st, owner); break;
+    case 2: face_flux_f<N, 2>(m, g, k, S, Sf, SF, c, info, ff, uf, gf, st, owner); break;
+    case 3: face_flux_f<N, 3>(m, g, k, S, Sf, SF, c, info, ff, uf, gf, st, owner); break;
+    case 4: face_flux_f<N, 4>(m, g, k, S, Sf, SF, c, info, ff, uf, gf, st, owner); break;
+    default: face_flux_f<N, 5>(m, g, k, S, Sf, SF, c, info, ff, uf, gf, st, owner); break;
   }
   if (owner) {
 #pragma unroll
@@ -1115,10 +1136,13 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
     for (int j = 0; j < 3; j++) st_all[i][j] = 0.0f;
 #pragma unroll
   for (int i = 0; i < N; ++i) {
+    // the material pressure only enters the FP32 stress: recovered in double-float
     const float ael = elastic_energy_f(G, Gmag, k.mu_f[i]);
-    const double p = ((k.gamma[i] - 1.0) * (s[C::i4 + i] - (double)ael) / at[i]) - k.gpi[i];
-    avf[i] = (float)at[i];
-    eos_stress_f(st_all, avf[i], (float)p, G, Gmag, k.mu_f[i], ast[i]);
+    const df a_d = df_from_double(at[i]);
+    const df p = df_sub(df_div(df_mul(k.gm1_d[i], df_add_f(df_from_double(s[C::i4 + i]), -ael)), a_d),
+                        k.gpi_d[i]);
+    avf[i] = a_d.hi;
+    eos_stress_f(st_all, avf[i], df_to_float(p), G, Gmag, k.mu_f[i], ast[i]);
   }
   double rhs[NA];
   float rhsA[9], nc[N - 1 + N + 9];
@@ -1268,11 +1292,12 @@ void ffv_m5f_recon(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, con
 }
 
 void ffv_m5f_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
-                  const float *SFf, float *FFf, float *UFf, double *GF, unsigned *status,
+                  const float *Sf, const float *SFf, float *FFf, float *UFf, double *GF,
+                  unsigned *status,
                   cudaStream_t st) {
   const unsigned blocks = (unsigned)((6 * m.n + 127) / 128);
-  if (k.nmat == 2) m5f_face_flux<2><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, FFf, UFf, GF, status);
-  else m5f_face_flux<3><<<blocks, 128, 0, st>>>(m, g, k, S, SFf, FFf, UFf, GF, status);
+  if (k.nmat == 2) m5f_face_flux<2><<<blocks, 128, 0, st>>>(m, g, k, S, Sf, SFf, FFf, UFf, GF, status);
+  else m5f_face_flux<3><<<blocks, 128, 0, st>>>(m, g, k, S, Sf, SFf, FFf, UFf, GF, status);
 }
 
 void ffv_m5f_cell_update(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,

@@ -1629,7 +1629,9 @@ static void stage_impl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k,
     }
     rec(f32 ? "m5f_recon_face" : k_names[0]);
   }
-  if (f32) ffv_m5f_flux(m, g, k, b.S, SFf, FFf, UFf, b.GF, b.status, st);
+  if (f32)
+    ffv_m5f_flux(m, g, k, b.S, k.order == 2 ? (const float *)b.RHS : nullptr, SFf, FFf, UFf, b.GF,
+                 b.status, st);
   else m5_face_flux<N><<<gf, tpb, 0, st>>>(m, g, k, b.S, b.SF, b.FF, b.UF, b.GF, b.status);
   rec(f32 ? "m5f_face_flux" : k_names[1]);
   if (f32)
