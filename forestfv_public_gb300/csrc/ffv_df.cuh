@@ -5,11 +5,11 @@
 // recovery: differences of ~1e9 numbers, divisions by volume fractions down to 1e-8) but not
 // the FP64 pipe, which GB300 runs at 1/64 of the FP32 rate.  The building blocks are the
 // error-free transformations of Knuth (TwoSum), Dekker (FastTwoSum) and the FMA-based
-// TwoProduct; addition with the error terms of both parts (accurate under cancellation),
-// multiplication and division as in the published double-double algorithms (Hida, Li and
-// Bailey, "Algorithms for quad-double precision floating point arithmetic", 2001), here on
-// FP32 pairs.  Exponent range is FP32's: every quantity held this way must stay within
-// about 1e-38..3e38 (energies ~1e11, pressures ~1e10, fractions >= 1e-8 here).
+// TwoProduct; addition, multiplication and division as in the published double-double
+// algorithms (Hida, Li and Bailey, "Algorithms for quad-double precision floating point
+// arithmetic", 2001), here on FP32 pairs.  Exponent range is FP32's: every quantity held
+// this way must stay within about 1e-38..3e38 (energies ~1e11, pressures ~1e10, fractions
+// >= 1e-8 here).
 #pragma once
 
 struct df {
@@ -40,11 +40,13 @@ __device__ __forceinline__ df two_prod(float a, float b) {
   return df{p, __fmaf_rn(a, b, -p)};
 }
 
+// addition with the leading parts' error term and the sum of the low parts (the "sloppy"
+// double-double addition): its error is below ~2^-46 of the larger operand, the order of the
+// pairs' own representation error, at about half the instructions of the variant that
+// carries the low parts' error term too
 __device__ __forceinline__ df df_add(df x, df y) {
   const df s = two_sum(x.hi, y.hi);
-  const df t = two_sum(x.lo, y.lo);
-  df u = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
-  return fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+  return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo)));
 }
 
 __device__ __forceinline__ df df_neg(df x) { return df{-x.hi, -x.lo}; }

@@ -692,7 +692,8 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
     for (int iv = 0; iv < N; ++iv)
       if (df_lt(k.oneeps_d, avf[iv])) irelax = false;
     if (irelax) {
-      df p0 = df_make(0.0f), sum0 = df_make(-1.0f);
+      df sum0 = df_make(-1.0f);
+      float p0 = 0.0f;  // the Newton iteration's start, FP32 is enough
       float a0[N], pkf[N], pif[N], b0[N], ig[N], e[N], plo[N], preset[N];
       bool live[N];
 #pragma unroll
@@ -705,12 +706,13 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
           if (df_le(pk, k.floor_d[iv])) pk = k.floor_d[iv];
           sum0 = df_add(sum0, avf[iv]);
         }
-        p0 = df_add(p0, df_mul(avf[iv], pk));
         a0[iv] = df_to_float(avf[iv]);
         pkf[iv] = df_to_float(pk);
+        p0 += a0[iv] * pkf[iv];
         pif[iv] = k.pinf_f[iv];
-        // at a material's pressure floor pk + p_inf is a few Pa beside 6e8
-        b0[iv] = df_to_float(df_div(df_make(1.0f), df_add(pk, k.pinf_d[iv])));
+        // at a material's pressure floor pk + p_inf is a few Pa beside 6e8: the sum in
+        // double-float, its reciprocal in FP32
+        b0[iv] = 1.0f / df_to_float(df_add(pk, k.pinf_d[iv]));
         ig[iv] = k.igam_f[iv];
         plo[iv] = k.plo_f[iv];
         preset[iv] = k.preset_f[iv];
@@ -725,7 +727,7 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
       // p_inf = 6e8 turns into ~200 Pa.  The iterate settles within a few steps; the cap
       // bounds the loop.
       const float F0 = df_to_float(sum0);
-      float pf = df_to_float(p0), F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
+      float pf = p0, F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
 #pragma unroll 1
       for (int iter = 0; iter < 64; iter++) {
         const float step = F / dF;
