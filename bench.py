@@ -477,17 +477,17 @@ def timed_amr_loop(solver, amr, dt, steps, warmup, stream, host=False):
     h2d = d2h = 0
     if host:
         buf = torch.empty((solver.neq, solver.mesh.n), dtype=torch.float64, pin_memory=True).numpy()
-        buf[:] = solver.download_state()
+        solver.download_state(out=buf)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
         e0.record(stream)
     for _ in range(steps):
         if host:
-            if buf.shape[1] != solver.mesh.n:
+            if buf.shape[1] != solver.mesh.n:  # the previous step's regrid changed the mesh
                 buf = torch.empty((solver.neq, solver.mesh.n), dtype=torch.float64,
                                   pin_memory=True).numpy()
-                buf[:] = solver.download_state()
+                solver.download_state(out=buf)
             solver.upload_state(buf)
             h2d += buf.nbytes
         amr.run(dt, 1)
@@ -495,7 +495,7 @@ def timed_amr_loop(solver, amr, dt, steps, warmup, stream, host=False):
             if buf.shape[1] != solver.mesh.n:
                 buf = torch.empty((solver.neq, solver.mesh.n), dtype=torch.float64,
                                   pin_memory=True).numpy()
-            buf[:] = solver.download_state()
+            solver.download_state(out=buf)
             d2h += buf.nbytes
     with torch.cuda.stream(stream):
         e1.record(stream)
@@ -610,7 +610,7 @@ def run_ours(args) -> None:
     for _ in range(e2e_steps):
         solver.upload_state(host)
         solver.step(dt, 1)
-        host[:] = solver.download_state()
+        solver.download_state(out=host)
     e2e_s = time.perf_counter() - t0
     e2e64 = {"value": world * mesh.n * e2e_steps / e2e_s, "unit": UNIT,
              "h2d_bytes_per_step": neq * 8 * mesh.n, "d2h_bytes_per_step": neq * 8 * mesh.n,

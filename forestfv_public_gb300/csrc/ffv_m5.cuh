@@ -62,8 +62,12 @@ void ffv_m5f_cell_update(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &
                          double *SN, const float *FFf, const float *UFf, double *RHS,
                          double *Snew, uint8_t *flag, const double *dt, int irk, unsigned *status,
                          cudaStream_t st);
-// cell pressure relaxation with the Newton iteration in FP32 and the energy-consistent
-// pressure and internal energies in FP64
+// the indicator's fields of a model-5 state, F [5][n] float (log rho, log p, alpha_0, |u|,
+// von Mises stress; FP32 with double-float pressure recovery; ffv_mlp.cu gathers them)
+void ffv_m5f_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
+                              cudaStream_t st);
+// cell pressure relaxation: the Newton iteration in FP32, the pressure recovery and the
+// energy-consistent pressure and internal energies in double-float
 void ffv_m5f_relax_cell(int64_t n, const M5Consts &k, const double *Sin, double *Sout,
                         uint8_t *flag, unsigned *status, cudaStream_t st);
 void ffv_m5_cfl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
@@ -81,13 +85,11 @@ struct ffv_m5_tagc {
 void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, const double *S,
                  int32_t *SI, int32_t *SItmp, int32_t *split, cudaStream_t st);
 
-// fields of the learned refinement indicator, F [5][n] float (ffv_mlp.cu gathers them)
+// exported per-leaf fields, F [nf][n] double (ffv_export_fields)
 void ffv_m5_export_fields(int64_t n, const M5Consts &k, const double *S, double *F,
                           cudaStream_t st);
 void ffv_m0_export_fields(int64_t n, double gamma, double pinf, const double *S, double *F,
                           cudaStream_t st);
-void ffv_m5_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
-                             cudaStream_t st);
 
 // model 0 (ffv_m0_tags.cu): the relative-jump criterion on cell states and the indicator
 // fields (log rho, log p, 1, |u|, 0)

@@ -1276,6 +1276,65 @@ __global__ void __launch_bounds__(128) m5f_relax_cell(int64_t n, M5Consts k,
   if (st) atomicOr(status, st);
 }
 
+// the indicator's five per-cell fields (log rho, log p, alpha_0, |u|, von Mises stress) in
+// FP32 from the FP64 state: the volume fractions, internal energies and each material's
+// pressure recovery in double-float (the mixture pressure sum_k alpha_k p_k cancels
+// (gamma_k - 1) alpha rho e_k against alpha_k gamma_k p_inf_k), the stress deviator in FP32
+template <int N>
+__global__ void __launch_bounds__(128) m5f_indicator_fields(int64_t n, M5Consts k,
+                                                            const double *__restrict__ S,
+                                                            float *__restrict__ F) {
+  using C = K5<N>;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  float r = 0.0f;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) r += (float)S[(int64_t)(C::i0 + iv) * n + c];
+  const float mx = (float)S[(int64_t)C::i1 * n + c], my = (float)S[(int64_t)(C::i1 + 1) * n + c],
+              mz = (float)S[(int64_t)(C::i1 + 2) * n + c];
+  df at[N];
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) at[i] = df_from_double(S[(int64_t)(C::i3 + i) * n + c]);
+  avf_limit_df<N>(k, at);
+  df sum = df_make(0.0f);
+#pragma unroll
+  for (int i = 0; i < N - 1; ++i) sum = df_add(sum, at[i]);
+  at[N - 1] = df_sub(df_make(1.0f), sum);
+  float A[9], G[9], Gmag;
+#pragma unroll
+  for (int q = 0; q < 9; q++) A[q] = (float)S[(int64_t)(C::i5 + q) * n + c];
+  gmat_f(A, G, Gmag);
+  float st[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
+  df p = df_make(0.0f);
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    const float ael = elastic_energy_f(G, Gmag, k.mu_f[i]);
+    const df pk = df_sub(df_div(df_mul(k.gm1_d[i], df_add_f(df_from_double(S[(int64_t)(C::i4 + i) * n + c]), -ael)),
+                                at[i]),
+                         k.gpi_d[i]);
+    p = df_add(p, df_mul(at[i], pk));
+    // the von Mises stress depends on the deviator only, to which -alpha_k p_k I adds
+    // nothing: the elastic part alone (in FP32 the isotropic terms, up to ~1e10 for a nearly
+    // absent material, would round away the deviator)
+    eos_stress_f(st, 0.0f, 0.0f, G, Gmag, k.mu_f[i], nullptr);
+  }
+  const float tr = (st[0][0] + st[1][1] + st[2][2]) * (1.0f / 3.0f);
+  float j2 = 0.0f;
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      const float d = st[i][j] - (i == j ? tr : 0.0f);
+      j2 += d * d;
+    }
+  const float pf = df_to_float(p);
+  F[c] = logf(fmaxf(r, 1e-30f));
+  F[n + c] = logf(fmaxf(pf, 1.0f));
+  F[2 * n + c] = df_to_float(at[0]);
+  F[3 * n + c] = sqrtf(mx * mx + my * my + mz * mz) / r;
+  F[4 * n + c] = sqrtf(1.5f * j2);
+}
+
 }  // namespace
 
 void ffv_m5f_shadow(int64_t n, const M5Consts &k, const double *S, float *Sf, cudaStream_t st) {
@@ -1311,6 +1370,13 @@ void ffv_m5f_cell_update(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &
     m5f_cell_update<2><<<blocks, 128, 0, st>>>(m, g, k, S, SN, FFf, UFf, RHS, Snew, flag, dt, irk, status);
   else
     m5f_cell_update<3><<<blocks, 128, 0, st>>>(m, g, k, S, SN, FFf, UFf, RHS, Snew, flag, dt, irk, status);
+}
+
+void ffv_m5f_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
+                              cudaStream_t st) {
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+  if (k.nmat == 2) m5f_indicator_fields<2><<<blocks, 128, 0, st>>>(n, k, S, F);
+  else m5f_indicator_fields<3><<<blocks, 128, 0, st>>>(n, k, S, F);
 }
 
 void ffv_m5f_relax_cell(int64_t n, const M5Consts &k, const double *Sin, double *Sout,

@@ -1453,38 +1453,6 @@ __global__ void __launch_bounds__(128) m5_tag_split(ffv_dmesh m, M5Consts k, ffv
   split[c] = level;
 }
 
-// per-cell fields of the learned indicator: log rho, log max(p, 1 Pa), alpha_0, |u|, von
-// Mises equivalent of the mixture stress (make_sol of the cell state)
-template <int N>
-__global__ void __launch_bounds__(128) m5_indicator_fields(int64_t n, M5Consts k,
-                                                           const double *__restrict__ S,
-                                                           float *__restrict__ F) {
-  using C = K5<N>;
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  double s[C::NEQ];
-  load_state<N>(S, n, c, s);
-  Sol<N> q;
-  make_sol<N>(k, s, s, false, q);
-  double p = 0.0;
-#pragma unroll
-  for (int iv = 0; iv < N; ++iv) p += q.avf[iv] * q.p[iv];
-  const double tr = (q.st[0][0] + q.st[1][1] + q.st[2][2]) / 3.0;
-  double j2 = 0.0;
-#pragma unroll
-  for (int i = 0; i < 3; i++)
-#pragma unroll
-    for (int j = 0; j < 3; j++) {
-      const double d = q.st[i][j] - (i == j ? tr : 0.0);
-      j2 += d * d;
-    }
-  F[c] = (float)log(q.r > 1e-300 ? q.r : 1e-300);
-  F[n + c] = (float)log(p > 1.0 ? p : 1.0);
-  F[2 * n + c] = (float)q.avf[0];
-  F[3 * n + c] = (float)sqrt(q.u * q.u + q.v * q.v + q.w * q.w);
-  F[4 * n + c] = (float)sqrt(1.5 * j2);
-}
-
 // exported fields (FP64): rho, u, v, w, sum_k alpha_k p_k, alpha_k, p_k, von Mises stress
 // of the reference's cell primitives (make_sol of the cell state)
 template <int N>
@@ -1553,13 +1521,6 @@ void ffv_m5_export_fields(int64_t n, const M5Consts &k, const double *S, double 
   const unsigned gc = (unsigned)((n + 127) / 128);
   if (k.nmat == 2) m5_export_fields<2><<<gc, 128, 0, st>>>(n, k, S, F);
   else m5_export_fields<3><<<gc, 128, 0, st>>>(n, k, S, F);
-}
-
-void ffv_m5_indicator_fields(int64_t n, const M5Consts &k, const double *S, float *F,
-                             cudaStream_t st) {
-  const unsigned gc = (unsigned)((n + 127) / 128);
-  if (k.nmat == 2) m5_indicator_fields<2><<<gc, 128, 0, st>>>(n, k, S, F);
-  else m5_indicator_fields<3><<<gc, 128, 0, st>>>(n, k, S, F);
 }
 
 void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, const double *S,

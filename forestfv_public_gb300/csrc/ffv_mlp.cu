@@ -65,30 +65,52 @@ __device__ __forceinline__ int64_t face_step(const ffv_dmesh &m, int64_t c, int 
   return s;
 }
 
-__global__ void __launch_bounds__(128) mlp_gather(ffv_dmesh m, const float *__restrict__ F,
-                                                  const float *__restrict__ norm,
-                                                  bf16 *__restrict__ X) {
-  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= m.n) return;
-  float mean[5], istd[5];
+// A block builds its 128 feature rows in shared memory (row stride 146 BF16 = 73 words,
+// odd, so that the threads' 4-byte accesses to their own rows fall in distinct banks) and
+// then writes them out as one contiguous run of 4-byte words: a thread writing its own
+// 288-byte row directly would touch 32 cache lines per warp store.
+constexpr int GATHER_TPB = 128, GATHER_SW = 73;  // shared words per row (KIN / 2 = 72, +1)
+__global__ void __launch_bounds__(GATHER_TPB) mlp_gather(ffv_dmesh m, const float *__restrict__ F,
+                                                         const float *__restrict__ norm,
+                                                         bf16 *__restrict__ X) {
+  __shared__ uint32_t tile[GATHER_TPB * GATHER_SW];
+  const int64_t c0 = (int64_t)blockIdx.x * GATHER_TPB;
+  const int64_t c = c0 + threadIdx.x;
+  if (c < m.n) {
+    float mean[5], istd[5];
 #pragma unroll
-  for (int q = 0; q < 5; q++) {
-    mean[q] = norm[q];
-    istd[q] = 1.0f / norm[5 + q];
+    for (int q = 0; q < 5; q++) {
+      mean[q] = norm[q];
+      istd[q] = 1.0f / norm[5 + q];
+    }
+    uint32_t *row = tile + threadIdx.x * GATHER_SW;
+    bf16 carry = __float2bfloat16_rn(0.0f);
+    int k = 0;  // feature index
+#pragma unroll 1
+    for (int o = 0; o < 27; o++) {
+      const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = o / 9 - 1;
+      int64_t e = c;
+      if (dx) e = face_step(m, e, dx < 0 ? 0 : 2);
+      if (dy) e = face_step(m, e, dy < 0 ? 3 : 1);
+      if (dz) e = face_step(m, e, dz < 0 ? 4 : 5);
+#pragma unroll
+      for (int q = 0; q < 5; q++, k++) {
+        const bf16 v = __float2bfloat16_rn((F[(int64_t)q * m.n + e] - mean[q]) * istd[q]);
+        if (k & 1) row[k >> 1] = pack2(carry, v);
+        else carry = v;
+      }
+    }
+    // k == 135: the last feature and the zero padding up to 144
+    row[NIN >> 1] = pack2(carry, __float2bfloat16_rn(0.0f));
+#pragma unroll
+    for (int w = (NIN >> 1) + 1; w < KIN / 2; w++) row[w] = 0u;
   }
-  bf16 *row = X + c * KIN;
-  for (int o = 0; o < 27; o++) {
-    const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = o / 9 - 1;
-    int64_t e = c;
-    if (dx) e = face_step(m, e, dx < 0 ? 0 : 2);
-    if (dy) e = face_step(m, e, dy < 0 ? 3 : 1);
-    if (dz) e = face_step(m, e, dz < 0 ? 4 : 5);
-#pragma unroll
-    for (int q = 0; q < 5; q++)
-      row[o * 5 + q] = __float2bfloat16_rn((F[(int64_t)q * m.n + e] - mean[q]) * istd[q]);
-  }
-#pragma unroll
-  for (int i = NIN; i < KIN; i++) row[i] = __float2bfloat16_rn(0.0f);
+  __syncthreads();
+  const int64_t rows = m.n - c0 < GATHER_TPB ? m.n - c0 : GATHER_TPB;
+  const int words = (int)rows * (KIN / 2);
+  uint32_t *dst = reinterpret_cast<uint32_t *>(X + c0 * KIN);
+  for (int w = threadIdx.x; w < words; w += GATHER_TPB)
+    dst[w] = tile[(w / (KIN / 2)) * GATHER_SW + w % (KIN / 2)];
 }
 
 // ------------------------------------------------------------------------- weights
@@ -587,7 +609,7 @@ int view(ffv_ctx *ctx, CtxView &v) {
   return ffv_ctx_view(ctx, &v.device, &v.st, &v.dm, &v.S, &v.k, &v.model, &v.gamma0, &v.pinf0);
 }
 void launch_fields(const CtxView &v, float *F) {
-  if (v.model == 5) ffv_m5_indicator_fields(v.dm.n, *v.k, v.S, F, v.st);
+  if (v.model == 5) ffv_m5f_indicator_fields(v.dm.n, *v.k, v.S, F, v.st);
   else ffv_m0_indicator_fields(v.dm.n, v.gamma0, v.pinf0, v.S, F, v.st);
 }
 }  // namespace

@@ -9,6 +9,8 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <functional>
+#include <queue>
 #include <vector>
 
 #include "ffv_internal.h"
@@ -58,38 +60,69 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
     return mx - split[c] > 1 ? mx - 1 : split[c];
   };
   // A sweep updates split in place in leaf order, each leaf seeing its predecessors' new
-  // values.  If no leaf would change when every leaf is evaluated on the values before the
-  // sweep, the in-place sweep changes nothing either (each leaf then sees exactly those
-  // values): that test runs on all host threads and skips the sequential sweep.
-  auto would_change = [&](auto rule) {
-    std::vector<char> hit(nth, 0);
+  // values.  It runs as a worklist with the same result: all leaves are first evaluated on
+  // the sweep's input in parallel, and those whose value would change are visited in leaf
+  // order; when a visited leaf changes, the later leaves that read its value (its sibling
+  // group for the coarsening rule, its face neighbours for the 2:1 rule) join the worklist.
+  // A leaf never on the list sees, when the sweep reaches it, exactly the inputs of the
+  // parallel evaluation, so its value does not change -- as in the full sweep.  Earlier
+  // leaves that read a changed value are not revisited in this sweep (the full sweep has
+  // passed them too); the next pass's parallel evaluation finds them.
+  std::vector<uint8_t> queued(n, 0);
+  auto sweep = [&](auto rule, bool sibling_deps) -> bool {
+    std::vector<std::vector<int64_t>> found(nth);
     parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
-      for (int64_t c = a; c < b && !hit[t]; c++)
-        if (rule(c) != split[c]) hit[t] = 1;
+      for (int64_t c = a; c < b; c++)
+        if (rule(c) != split[c]) found[t].push_back(c);
     });
-    for (char h : hit)
-      if (h) return true;
-    return false;
+    std::priority_queue<int64_t, std::vector<int64_t>, std::greater<int64_t>> work;
+    for (auto &v : found)
+      for (int64_t c : v) {
+        work.push(c);
+        queued[c] = 1;
+      }
+    if (work.empty()) return false;
+    bool changed = false;
+    auto push_later = [&](int64_t d, int64_t cur) {
+      if (d > cur && !queued[d]) {
+        queued[d] = 1;
+        work.push(d);
+      }
+    };
+    while (!work.empty()) {
+      const int64_t c = work.top();
+      work.pop();
+      queued[c] = 0;
+      const int32_t v = rule(c);
+      if (v == split[c]) continue;
+      split[c] = v;
+      changed = true;
+      if (sibling_deps) {
+        const int64_t g = group[c];
+        if (g >= 0)
+          for (int64_t q = g; q < g + 8; q++) push_later(q, c);
+      } else {
+        const uint32_t info = m->info[c];
+        for (int f = 0; f < 6; f++) {
+          const uint32_t kind = ffv_face_kind(info, f);
+          if (kind & FFV_FK_BC) continue;
+          const int32_t s = m->nbr[6 * c + f];
+          if (kind == FFV_FK_FINER) {
+            for (int q = 0; q < 4; q++) push_later(m->sub[4 * (int64_t)s + q], c);
+          } else {
+            push_later(s, c);
+          }
+        }
+      }
+    }
+    return changed;
   };
   // A pass is a function of `split` alone: once one changes nothing, every later pass
   // would see the same input and change nothing either, so the passes end there.
   for (int32_t pass = 0; pass < level_max + 1; pass++) {
-    bool changed = false;
-    if (would_change(rule1)) {
-      for (int64_t c = 0; c < n; c++) {
-        const int32_t v = rule1(c);
-        changed |= v != split[c];
-        split[c] = v;
-      }
-    }
-    if (would_change(rule2)) {
-      for (int64_t c = 0; c < n; c++) {
-        const int32_t v = rule2(c);
-        changed |= v != split[c];
-        split[c] = v;
-      }
-    }
-    if (!changed) break;
+    const bool c1 = sweep(rule1, true);
+    const bool c2 = sweep(rule2, false);
+    if (!c1 && !c2) break;
   }
   return FFV_OK;
 }

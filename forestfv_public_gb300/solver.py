@@ -85,11 +85,16 @@ class Solver:
         _lib.check(_lib.lib().ffv_upload_state(self._h, S.ctypes.data, self.mesh.n, self.neq),
                    "ffv_upload_state")
 
-    def download_state(self) -> np.ndarray:
-        S = np.empty((self.neq, self.mesh.n))
-        _lib.check(_lib.lib().ffv_download_state(self._h, S.ctypes.data, self.mesh.n, self.neq),
+    def download_state(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The state [neq, n]; into `out` when given (a pinned host buffer copies at the
+        link's full rate, a fresh pageable array goes through the driver's staging)."""
+        if out is None:
+            out = np.empty((self.neq, self.mesh.n))
+        assert out.shape == (self.neq, self.mesh.n) and out.dtype == np.float64
+        assert out.flags["C_CONTIGUOUS"]
+        _lib.check(_lib.lib().ffv_download_state(self._h, out.ctypes.data, self.mesh.n, self.neq),
                    "ffv_download_state")
-        return S
+        return out
 
     def rk(self, irk: int, dt: float) -> None:
         _lib.check(_lib.lib().ffv_stage(self._h, irk, dt), "ffv_stage")

@@ -148,3 +148,33 @@ def test_features_match_oracle(built_lib):
     assert np.abs(X[:, :mlp.NIN] - ref).max() <= 1e-2 * max(1.0, np.abs(ref).max())
     ind.close()
     s.close()
+
+
+def test_fields_match_host_eos(built_lib):
+    """The indicator's per-cell fields (FP32 with double-float pressure recovery) against the
+    host float64 restatement of the reference's equation of state."""
+    from forestfv_public_gb300.fields import primitives
+    g = load_golden("m5_wall_amr")
+    m = mesh_from_golden(g)
+    q = m5_params(g)
+    s = Solver(model=5, gamma=q["gamma"], pinf=q["pinf"], mu=q["mu"], amin=q["amin"],
+               avf_lim=q["avf_lim"], prelax=q["prelax"])
+    s.set_mesh(m)
+    S = np.ascontiguousarray(g["S_final"].T)
+    s.upload_state(S)
+    ind = Indicator()
+    F = ind.fields(s).cpu().numpy().astype(np.float64)
+    ref = primitives(S, q["gamma"], q["pinf"], q["mu"], q["amin"])
+    N = len(q["gamma"])
+    u = np.linalg.norm(S[N:N + 3], axis=0) / ref["rho"]
+    assert np.abs(F[0] - np.log(ref["rho"])).max() <= 1e-6
+    hi = ref["p"] > 100.0  # below, log max(p, 1 Pa) of near-floor pressures is ill-conditioned
+    assert np.abs(F[1][hi] - np.log(ref["p"][hi])).max() <= 1e-4
+    assert np.abs(F[2] - ref["alpha"][0]).max() <= 1e-6
+    assert np.abs(F[3] - u).max() <= 1e-5 * max(1.0, u.max())
+    # the FP32 elastic deviator: for strains ~1e-6, dev(G^2) - |G|^(1/3) dev(G) is a
+    # difference of O(1) numbers, resolved to ~1 % in FP32 -- ample for a network input
+    assert np.abs(F[4] - ref["vm"]).max() <= 1e-2 * max(1.0, ref["vm"].max())
+    assert np.all(F[4][ref["vm"] == 0.0] == 0.0)
+    ind.close()
+    s.close()
