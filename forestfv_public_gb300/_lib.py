@@ -77,7 +77,7 @@ EXPORTS = (
     "ffv_destroy", "ffv_set_mesh", "ffv_upload_state", "ffv_download_state", "ffv_stage",
     "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
     "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
-    "ffv_tags", "ffv_tags_raw", "ffv_tags_missed", "ffv_tags_smooth", "ffv_adapt", "ffv_adapt_map", "ffv_adapt_changes", "ffv_mesh_leaves",
+    "ffv_tags", "ffv_tags_raw", "ffv_tags_missed", "ffv_tags_smooth", "ffv_adapt", "ffv_adapt_map", "ffv_adapt_changes", "ffv_mesh_adapt", "ffv_mesh_leaves",
     "ffv_checkpoint_write", "ffv_checkpoint_info", "ffv_checkpoint_read", "ffv_restart_text_write",
     "ffv_restart_text_info", "ffv_restart_text_read", "ffv_tecplot_write", "ffv_export_fields",
     "ffv_mlp_create", "ffv_mlp_destroy", "ffv_mlp_get_params", "ffv_mlp_set_params",
@@ -125,6 +125,7 @@ def lib() -> ctypes.CDLL:
     L.ffv_adapt.argtypes = [vp, vp, vp, ctypes.POINTER(vp)]
     L.ffv_mesh_leaves.argtypes = [vp, vp, vp, vp]
     L.ffv_adapt_map.argtypes = [vp, vp, vp, ctypes.POINTER(vp), vp]
+    L.ffv_mesh_adapt.argtypes = [vp, vp, ctypes.POINTER(vp), vp]
     L.ffv_adapt_changes.argtypes = [vp, vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]
     u64, f32 = ctypes.c_uint64, ctypes.c_float
     cp = ctypes.c_char_p

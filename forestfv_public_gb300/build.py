@@ -28,6 +28,7 @@ SOURCES = {
     "ffv_mesh.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "ffv_tags.cpp": [],
     "ffv_io.cpp": [],
+    "ffv_regrid.cpp": [],
     "ffv_api.cu": [],
     "ffv_m0_fp64.cu": ["--fmad=false"],
     "ffv_m5_fp64.cu": ["--fmad=false"],

@@ -7,8 +7,9 @@
 // (merge.c:52-57); a leaf that wants a finer level splits into its eight children, which
 // copy its state (split.c:424-427); every other leaf is kept.  Merges and splits exclude
 // each other (all eight below their level vs. above it), so one sweep in leaf order does
-// both of the reference's loops.  The new leaves go through ffv_mesh_build; the context
-// then holds the new tables and the carried-over state.
+// both of the reference's loops.  The new leaves and tables come from ffv_mesh_adapt (the
+// host rebuild around the changed leaves); the context then holds the new tables and the
+// carried-over state.
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -46,9 +47,10 @@ __global__ void adapt_remap(int64_t n_new, int64_t n_old, int neq, const int64_t
 int ffv_ctx_adapt_view(ffv_ctx *ctx, int *device, cudaStream_t *st, int64_t *n, int *neq,
                        double **d_S, int *model, const M5Consts **k);
 extern "C" int ffv_set_mesh(ffv_ctx *c, const ffv_mesh *m);
-extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves, const int32_t *tree_ijk,
-                              const int32_t *level, const int32_t *cell_ijk, ffv_mesh **out,
-                              int64_t *order_out);
+extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh **out,
+                              int64_t *src);
+extern "C" int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit,
+                                 int64_t *nmerge);
 extern "C" void ffv_mesh_free(ffv_mesh *m);
 int ffv_ctx_mark_state(ffv_ctx *ctx);
 
@@ -64,82 +66,21 @@ extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *spl
   int rc = ffv_ctx_adapt_view(ctx, &device, &st, &n, &neq, &d_S, &model, &k);
   if (rc != FFV_OK) return rc;
   if (n != m->n) return FFV_ERR_ARG;
-  // what becomes of each old leaf: 8 split (eight leaves out), 1 kept, 2 the first of a
-  // merging group (its parent out), 0 the other seven of a merging group; then a prefix
-  // sum and the new leaf list written in parallel, in the order one sweep in leaf order
-  // gives
-  const int nth = host_threads();
-  std::vector<uint8_t> cnt(n);
-  std::vector<int64_t> tsum(nth + 1, 0), tmerged(nth, 0);
-  int bad = 0;
-  parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
-    int64_t acc = 0;
-    for (int64_t c = a; c < b; c++) {
-      const int l = ffv_info_level(m->info[c]);
-      const int64_t g = l > 1 ? ffv_sibling_group(m, c) : -1;
-      bool merge = g >= 0;
-      for (int q = 0; q < 8 && merge; q++) merge = split[g + q] < l;
-      uint8_t k;
-      if (merge) k = (g == c) ? 2 : 0;
-      else if (split[c] > l) k = 8;
-      else k = 1;
-      if (k == 8 && l + 1 > FFV_MAX_LEVEL) __atomic_store_n(&bad, 1, __ATOMIC_RELAXED);
-      if (k == 2) tmerged[t]++;
-      cnt[c] = k;
-      acc += k == 2 ? 1 : k;
-    }
-    tsum[t + 1] = acc;
-  });
-  if (bad) return FFV_ERR_TABLE;
-  for (int t = 0; t < nth; t++) tsum[t + 1] += tsum[t];
-  const int64_t n_out = tsum[nth];
-  int64_t nmerged = 0;
-  for (int t = 0; t < nth; t++) nmerged += tmerged[t];
-  std::vector<int32_t> tij(3 * n_out), lev(n_out), cij(3 * n_out);
-  std::vector<int64_t> map(n_out);
-  parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
-    int64_t o = tsum[t];
-    for (int64_t c = a; c < b; c++) {
-      if (cnt[c] == 0) continue;
-      const int l = ffv_info_level(m->info[c]);
-      const int32_t *tr = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
-      if (cnt[c] == 2) {  // merge.c: the parent of eight leaves
-        for (int d = 0; d < 3; d++) {
-          tij[3 * o + d] = tr[d];
-          cij[3 * o + d] = x[d] >> 1;
-        }
-        lev[o] = l - 1;
-        map[o] = -1 - c;
-        o++;
-      } else if (cnt[c] == 8) {  // split.c: eight children in child order, corner k at (bit1, bit0, bit2)
-        for (int q = 0; q < 8; q++, o++) {
-          for (int d = 0; d < 3; d++) tij[3 * o + d] = tr[d];
-          cij[3 * o] = 2 * x[0] + ((q >> 1) & 1);
-          cij[3 * o + 1] = 2 * x[1] + (q & 1);
-          cij[3 * o + 2] = 2 * x[2] + ((q >> 2) & 1);
-          lev[o] = l + 1;
-          map[o] = c;
-        }
-      } else {
-        for (int d = 0; d < 3; d++) {
-          tij[3 * o + d] = tr[d];
-          cij[3 * o + d] = x[d];
-        }
-        lev[o] = l;
-        map[o] = c;
-        o++;
-      }
-    }
-  });
-  const int64_t n_new = (int64_t)lev.size();
+  // the new leaves and their tables (host; rows of leaves the pass leaves alone are the old
+  // ones renumbered), then the state carried over on the device
   ffv_mesh *nm = nullptr;
-  std::vector<int64_t> order(n_new);
-  rc = ffv_mesh_build(&m->desc, n_new, tij.data(), lev.data(), cij.data(), &nm, order.data());
+  std::vector<int64_t> cmap;
+  {
+    int64_t ns = 0, nmg = 0;
+    rc = ffv_adapt_changes(m, split, &ns, &nmg);
+    if (rc != FFV_OK) return rc;
+    cmap.resize(m->n + 7 * (ns - nmg));
+  }
+  rc = ffv_mesh_adapt(m, split, &nm, cmap.data());
   if (rc != FFV_OK) return rc;
-  std::vector<int64_t> cmap(n_new);
-  parallel_chunks(n_new, nth, [&](int, int64_t a, int64_t b) {
-    for (int64_t j = a; j < b; j++) cmap[j] = map[order[j]];
-  });
+  const int64_t n_new = nm->n;
+  int64_t nmerged = 0;
+  for (int64_t j = 0; j < n_new; j++) nmerged += cmap[j] < 0 ? 1 : 0;
   if (src) memcpy(src, cmap.data(), sizeof(int64_t) * n_new);
   // carry the state over on the device, then swap the tables
   cudaError_t e = cudaSetDevice(device);

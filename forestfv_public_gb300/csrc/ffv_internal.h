@@ -52,6 +52,21 @@ struct ffv_level_geom {
 // some sibling is not a leaf (then the group is not in the table).  In the tables' cell
 // order (depth-first by child index) the eight children of a parent are consecutive, and
 // child k of a parent sits at cell coordinates 2p + (bit1 k, bit0 k, bit2 k).
+// Morton key whose base-8 digits are child indices (corner bit k: x = bit1, y = bit0,
+// z = bit2), so that sorting by it reproduces the depth-first child order; 21 bits a lane
+static inline uint64_t ffv_spread3(uint64_t v) {  // 21 bits -> every third bit
+  v &= 0x1fffffULL;
+  v = (v | v << 32) & 0x1f00000000ffffULL;
+  v = (v | v << 16) & 0x1f0000ff0000ffULL;
+  v = (v | v << 8) & 0x100f00f00f00f00fULL;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
+  v = (v | v << 2) & 0x1249249249249249ULL;
+  return v;
+}
+static inline uint64_t ffv_morton(uint32_t x, uint32_t y, uint32_t z) {
+  return (ffv_spread3(x) << 1) | ffv_spread3(y) | (ffv_spread3(z) << 2);
+}
+
 struct ffv_mesh;
 int64_t ffv_sibling_group(const ffv_mesh *m, int64_t c);
 

@@ -61,16 +61,6 @@ uint64_t fnv1a(uint64_t h, const void *p, size_t len) {
 }
 const uint64_t kFnvBasis = 0xCBF29CE484222325ull;
 
-uint64_t spread3(uint32_t v) {
-  uint64_t x = v & 0x1FFFFF, out = 0;
-  for (int b = 0; b < 21; b++) out |= ((x >> b) & 1ull) << (3 * b);
-  return out;
-}
-// child-index Morton key of (x, y, z): digit = (bit of x) << 1 | (bit of y) | (bit of z) << 2
-uint64_t mkey(uint32_t x, uint32_t y, uint32_t z) {
-  return (spread3(x) << 1) | spread3(y) | (spread3(z) << 2);
-}
-
 // trees in Morton order of their coordinates: rank -> (i, j, k) and (i, j, k) -> rank
 struct TreeOrder {
   std::vector<int32_t> ijk;   // [3 T] by rank
@@ -84,7 +74,7 @@ struct TreeOrder {
       const int32_t i = (int32_t)(t / ((int64_t)nt[1] * nt[2]));
       const int32_t j = (int32_t)((t / nt[2]) % nt[1]);
       const int32_t l = (int32_t)(t % nt[2]);
-      k[t] = {mkey(i, j, l), t};
+      k[t] = {ffv_morton(i, j, l), t};
     }
     std::sort(k.begin(), k.end());
     ijk.resize(3 * T);

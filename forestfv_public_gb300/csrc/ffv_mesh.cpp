@@ -103,24 +103,8 @@ int axis_of(const V3 &v, int8_t *axis, int8_t *sign) {
   return 0;
 }
 
-uint64_t spread3(uint64_t v) {  // 21 bits -> every third bit
-  v &= 0x1fffffULL;
-  v = (v | v << 32) & 0x1f00000000ffffULL;
-  v = (v | v << 16) & 0x1f0000ff0000ffULL;
-  v = (v | v << 8) & 0x100f00f00f00f00fULL;
-  v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
-  v = (v | v << 2) & 0x1249249249249249ULL;
-  return v;
-}
-
-// Morton key whose base-8 digits are child indices (corner bit k: x = bit1, y = bit0,
-// z = bit2), so that sorting by it reproduces the depth-first child order.
-uint64_t morton(uint32_t x, uint32_t y, uint32_t z) {
-  return (spread3(x) << 1) | spread3(y) | (spread3(z) << 2);
-}
-
 uint64_t cell_key(int level, uint32_t gx, uint32_t gy, uint32_t gz) {
-  return ((uint64_t)level << 60) | morton(gx, gy, gz);
+  return ((uint64_t)level << 60) | ffv_morton(gx, gy, gz);
 }
 
 // fn(t, c0, c1) over [0, n) in nthreads contiguous chunks, on nthreads host threads
@@ -222,9 +206,9 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
   parallel_chunks(nleaves, nthreads, [&](int, int64_t c0, int64_t c1) {
     for (int64_t i = c0; i < c1; i++) {
       perm[i] = i;
-      tkey[i] = morton(tree_ijk[3 * i], tree_ijk[3 * i + 1], tree_ijk[3 * i + 2]);
+      tkey[i] = ffv_morton(tree_ijk[3 * i], tree_ijk[3 * i + 1], tree_ijk[3 * i + 2]);
       int sh = D - (level[i] - 1);
-      lkey[i] = morton((uint32_t)cell_ijk[3 * i] << sh, (uint32_t)cell_ijk[3 * i + 1] << sh,
+      lkey[i] = ffv_morton((uint32_t)cell_ijk[3 * i] << sh, (uint32_t)cell_ijk[3 * i + 1] << sh,
                        (uint32_t)cell_ijk[3 * i + 2] << sh);
     }
   });

@@ -34,6 +34,20 @@ def adapt_changes(mesh: Mesh, split: np.ndarray) -> tuple[int, int]:
     return int(ns.value), int(nm.value)
 
 
+def mesh_adapt(mesh: Mesh, split: np.ndarray):
+    """The leaves and face tables of one refineh pass with targets `split` (host only,
+    ffv_mesh_adapt); returns (Mesh, src) with every new leaf's source."""
+    split = np.ascontiguousarray(split, dtype=np.int32)
+    ns, nm = adapt_changes(mesh, split)
+    src = np.empty(mesh.n + 7 * (ns - nm), np.int64)
+    h = ctypes.c_void_p()
+    _lib.check(_lib.lib().ffv_mesh_adapt(mesh.handle, split.ctypes.data, ctypes.byref(h),
+                                         src.ctypes.data), "ffv_mesh_adapt")
+    new = Mesh.from_handle(h, mesh.ntrees, mesh.bc, mesh.tree_edge)
+    assert src.shape[0] == new.n
+    return new, src
+
+
 def would_change(mesh: Mesh, split: np.ndarray) -> bool:
     """Whether a refineh pass with targets `split` changes any leaf: a leaf wants a finer
     level, or eight sibling leaves all want a coarser one (refineh.c:10-57)."""

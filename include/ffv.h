@@ -206,6 +206,11 @@ int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **
  * j..j+7.  n_new = n + 7 (nsplit - nmerge) with the counts of ffv_adapt_changes. */
 int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, ffv_mesh **out,
                   int64_t *src);
+/* The host half of ffv_adapt (no GPU): the leaves of one refineh pass with targets split[n]
+ * and their face tables -- equal to ffv_mesh_build's for those leaves, rebuilt only around
+ * the leaves that split or merge (the other rows are the old ones, renumbered).  src[n_new]
+ * (nullable) as ffv_adapt_map's. */
+int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh **out, int64_t *src);
 /* What one refineh pass with targets split[n] would do (host, no GPU): the number of
  * leaves that split and of sibling groups that merge.  Both 0: the pass changes nothing. */
 int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit, int64_t *nmerge);

@@ -1,6 +1,7 @@
 """Host logic of the adaptive time loop: whether a refineh pass changes any leaf (the early
 end of meshadaptation's rounds) and the level the gradient criteria assign."""
 import numpy as np
+import pytest
 
 from forestfv_public_gb300 import Mesh
 from forestfv_public_gb300._lib import TagParams
@@ -50,3 +51,37 @@ def test_carry_marks_children_and_parents():
     assert got.tolist() == [False] * 8 + [True, False, True]
     src = np.array([-1 - 2, 10], np.int64)  # old 2..9 merged (none marked), 10 kept
     assert carry_marks(src, marks).tolist() == [False, True]
+
+
+def _random_pass(m, rng, lmax):
+    from forestfv_public_gb300.solver import tags_smooth
+    tgt = m.level + rng.integers(-1, 2, m.n)
+    tgt = np.clip(tgt, 1, lmax).astype(np.int32)
+    return tags_smooth(m, lmax, tgt)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_mesh_adapt_equals_full_build(seed, built_lib):
+    """The incremental rebuild of a refineh pass gives the full builder's tables."""
+    from forestfv_public_gb300.mesh import Leaves
+    from forestfv_public_gb300.solver import mesh_adapt
+    from forestfv_public_gb300.workloads import refine_to_target
+    rng = np.random.default_rng(seed)
+    leaves = refine_to_target((2, 3, 2), 2, 4, lambda c, h: np.where(
+        c[:, 0] < 0.25, 4, np.where(c[:, 0] < 0.5, 3, 2)))
+    m = Mesh((2, 3, 2), leaves, bc=(2, 4, 1, 2, 3, 2), tree_edge=0.5)
+    for _ in range(4):
+        split = _random_pass(m, rng, 6)
+        new, src = mesh_adapt(m, split)
+        ref = Mesh(m.ntrees, Leaves(new.tree_ijk, new.level, new.cell_ijk), bc=m.bc,
+                   tree_edge=m.tree_edge)
+        assert np.array_equal(ref.order, np.arange(new.n))  # emitted in leaf order
+        e1, e2 = new.export(), ref.export()
+        for k in e1:
+            assert np.array_equal(e1[k], e2[k]), k
+        # sources: kept and split leaves point at their old leaf, merged parents at 8 siblings
+        lev_old = m.level
+        keep = src >= 0
+        assert np.all((new.level[keep] == lev_old[src[keep]]) | (new.level[keep] == lev_old[src[keep]] + 1))
+        assert np.all(new.level[~keep] == lev_old[-1 - src[~keep]] - 1)
+        m = new
