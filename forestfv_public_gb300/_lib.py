@@ -78,7 +78,7 @@ EXPORTS = (
     "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
     "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
     "ffv_tags", "ffv_tags_raw", "ffv_tags_missed", "ffv_tags_smooth", "ffv_adapt", "ffv_adapt_map", "ffv_adapt_changes", "ffv_mesh_adapt", "ffv_mesh_leaves",
-    "ffv_checkpoint_write", "ffv_checkpoint_info", "ffv_checkpoint_read", "ffv_restart_text_write",
+    "ffv_conservation_sums", "ffv_checkpoint_write", "ffv_checkpoint_info", "ffv_checkpoint_read", "ffv_restart_text_write",
     "ffv_restart_text_info", "ffv_restart_text_read", "ffv_tecplot_write", "ffv_export_fields",
     "ffv_mlp_create", "ffv_mlp_destroy", "ffv_mlp_get_params", "ffv_mlp_set_params",
     "ffv_mlp_set_norm", "ffv_mlp_fields", "ffv_mlp_features", "ffv_mlp_forward",
@@ -128,6 +128,7 @@ def lib() -> ctypes.CDLL:
     L.ffv_mesh_adapt.argtypes = [vp, vp, ctypes.POINTER(vp), vp]
     L.ffv_adapt_changes.argtypes = [vp, vp, ctypes.POINTER(i64), ctypes.POINTER(i64)]
     u64, f32 = ctypes.c_uint64, ctypes.c_float
+    L.ffv_conservation_sums.argtypes = [vp, vp]
     cp = ctypes.c_char_p
     L.ffv_checkpoint_write.argtypes = [cp, vp, vp, i32, i64, dbl]
     L.ffv_checkpoint_info.argtypes = [cp, ctypes.POINTER(ForestDesc), ctypes.POINTER(i64),

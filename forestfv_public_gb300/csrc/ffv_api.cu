@@ -510,6 +510,71 @@ int ffv_cfl_dt(ffv_ctx *c, double cfl, double *dt_out) {
   return FFV_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+constexpr int kSumBlocks = 152 * 4, kSumThreads = 256;
+
+// block b's partial of sum_c |V_c| S[v][c] over its grid-stride cells, for every variable:
+// a fixed assignment of cells to threads and a fixed reduction tree, so the sums are
+// reproducible bit for bit
+__global__ void __launch_bounds__(kSumThreads) sum_partials(ffv_dmesh m, ffv_geom g, int neq,
+                                                            const double *__restrict__ S,
+                                                            double *__restrict__ part) {
+  __shared__ double red[kSumThreads];
+  for (int v = 0; v < neq; v++) {
+    double acc = 0.0;
+    for (int64_t c = (int64_t)blockIdx.x * kSumThreads + threadIdx.x; c < m.n;
+         c += (int64_t)gridDim.x * kSumThreads)
+      acc += fabs(g.vol[ffv_info_level(m.info[c])]) * S[(int64_t)v * m.n + c];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = kSumThreads / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[(int64_t)v * gridDim.x + blockIdx.x] = red[0];
+    __syncthreads();
+  }
+}
+
+// one block per variable: the partials in a fixed order
+__global__ void __launch_bounds__(kSumThreads) sum_final(int nparts, const double *__restrict__ part,
+                                                         double *__restrict__ out) {
+  __shared__ double red[kSumThreads];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += kSumThreads) acc += part[(int64_t)blockIdx.x * nparts + i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = kSumThreads / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+}  // namespace
+
+extern "C" {
+
+int ffv_conservation_sums(ffv_ctx *c, double *sums) {
+  if (!c || !sums) return FFV_ERR_ARG;
+  if (!c->have_state) return FFV_ERR_STATE;
+  CK(cudaSetDevice(c->device));
+  double *d_part = nullptr;
+  CK(cudaMalloc(&d_part, sizeof(double) * ((size_t)kSumBlocks + 1) * c->neq));
+  double *d_out = d_part + (size_t)kSumBlocks * c->neq;
+  sum_partials<<<kSumBlocks, kSumThreads, 0, c->stream>>>(c->dm, c->geom, c->neq, c->d_S, d_part);
+  sum_final<<<c->neq, kSumThreads, 0, c->stream>>>(kSumBlocks, d_part, d_out);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(sums, d_out, sizeof(double) * c->neq, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_part);
+  return cuda_rc(e);
+}
+
 int ffv_state_device_ptr(ffv_ctx *c, double **d_S) {
   if (!c || !d_S) return FFV_ERR_ARG;
   if (!c->have_mesh) return FFV_ERR_STATE;

@@ -194,6 +194,14 @@ class Solver:
             self.adapt(split)
         return self.mesh
 
+    def conservation_sums(self) -> np.ndarray:
+        """sum over cells of |V| S[v] per conserved variable, FP64 on the device
+        (ffv_conservation_sums)."""
+        out = np.empty(self.neq)
+        _lib.check(_lib.lib().ffv_conservation_sums(self._h, out.ctypes.data),
+                   "ffv_conservation_sums")
+        return out
+
     def cfl_dt(self, cfl: float) -> float:
         out = ctypes.c_double()
         _lib.check(_lib.lib().ffv_cfl_dt(self._h, cfl, ctypes.byref(out)), "ffv_cfl_dt")

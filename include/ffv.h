@@ -217,6 +217,11 @@ int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit, 
 /* The leaves of a mesh in its cell order (tree_ijk[3n], level[n], cell_ijk[3n]). */
 int ffv_mesh_leaves(const ffv_mesh *m, int32_t *tree_ijk, int32_t *level, int32_t *cell_ijk);
 
+/* Global conservation sums in FP64: sums[v] = sum over leaves of |V| S[v] for every conserved
+ * variable (mass of each material, momentum, total energy, ...), a reproducible device
+ * reduction (fixed cell-to-thread assignment and reduction order). */
+int ffv_conservation_sums(ffv_ctx *ctx, double *sums);
+
 /* Checkpoint/restart and field export (host side, no GPU).
  *
  * Binary checkpoint (no counterpart in the reference): the leaves Morton-keyed (tree rank,
