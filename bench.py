@@ -199,6 +199,16 @@ WORKLOADS = {"config2": wl_config2, "config1": wl_config1, "config2m": wl_config
 
 
 # ------------------------------------------------------------------------------ helpers
+def max_over_ranks(t_ms: float, device) -> float:
+    """The slowest rank's time: with N ranks every rank runs its own replica of the
+    workload (the step does not shard here), and the whole job's rate is N replicas over
+    the slowest one's time."""
+    import torch
+    t = torch.tensor([t_ms], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -566,9 +576,7 @@ def run_ours(args) -> None:
     torch.cuda.synchronize(dev)
     t_ms = sum(a.elapsed_time(b) for a, b in ev)
     if world > 1:
-        t = torch.tensor([t_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_ms = float(t.item())
+        t_ms = max_over_ranks(t_ms, dev)
     value_fp64 = world * mesh.n * args.steps / (t_ms / 1e3)
 
     def kernel_times(s, nprof):

@@ -77,3 +77,29 @@ def test_m5_nan_wave_speed_reported(built_lib):
     with pytest.raises(FFVError) as e:
         s.step(float(g["dt"]), 3 * int(g["steps"]))
     assert e.value.code == 5
+
+
+def test_cfl_dt_model5(built_lib):
+    """ffv_cfl_dt (warp-shuffle min-reduction) against the host restatement:
+    dt = cfl * min over cells of h / (max_a |u_a| + c), c^2 = sum_k alpha_k gamma_k
+    (p_k + p_inf_k) / rho (the mixture sound speed of m5_wave_speeds.c:43-50)."""
+    from forestfv_public_gb300.fields import primitives
+    g = load_golden("m5_bubble_prelax3")
+    q = m5_params(g)
+    m = mesh_from_golden(g)
+    s = Solver(model=5, gamma=q["gamma"], pinf=q["pinf"], mu=q["mu"], amin=q["amin"],
+               avf_lim=q["avf_lim"], prelax=q["prelax"])
+    s.set_mesh(m)
+    S = np.ascontiguousarray(g["S_final"].T)
+    s.upload_state(S)
+    N = len(q["gamma"])
+    pr = primitives(S, q["gamma"], q["pinf"], q["mu"], q["amin"])
+    gam, pinf = np.asarray(q["gamma"]), np.asarray(q["pinf"])
+    p_k = np.stack([(gam[k] - 1.0) * S[2 * N + 3 + k] / pr["alpha"][k] - gam[k] * pinf[k]
+                    for k in range(N)])
+    c2 = (pr["alpha"] * gam[:, None] * (p_k + pinf[:, None])).sum(axis=0) / pr["rho"]
+    u = np.abs(S[N:N + 3] / pr["rho"]).max(axis=0)
+    h = 0.5 / (1 << (m.level - 1)).astype(np.float64)
+    ref = 0.3 * (h / (u + np.sqrt(c2))).min()
+    assert abs(s.cfl_dt(0.3) - ref) <= 1e-10 * ref
+    s.close()
