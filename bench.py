@@ -676,7 +676,7 @@ def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, ke
     tags = tuple(amr_cfg["tags"])
     every, thr = amr_cfg["every"], amr_cfg["threshold"]
     si_max = tags[13] if tags[11] == 1 else 0
-    judge_launches = (si_max + 1) if tags[11] == 1 else 2
+    judge_launches = (si_max + 2) if tags[11] == 1 else 3
 
     def fresh(precision):
         s = Solver(device=dev.index, precision=precision, **kw)

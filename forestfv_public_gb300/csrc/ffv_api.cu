@@ -29,6 +29,10 @@ struct ffv_ctx {
   M5Consts m5;
   // refinement tags
   int32_t *d_SI, *d_SItmp, *d_split;
+  double *d_tagpr;  // per-cell mixture pressure and density for the criterion [2][n]
+  // cells and subface groups the mesh buffers are allocated for (a new mesh that fits reuses
+  // them: a regrid then allocates nothing)
+  int64_t cap, cap_nsub;
   unsigned int *d_status;
   unsigned long long *d_red;
   // pinned host scalars
@@ -69,16 +73,50 @@ void free_mesh_buffers(ffv_ctx *c) {
   cudaFree(c->d_SI);
   cudaFree(c->d_SItmp);
   cudaFree(c->d_split);
+  cudaFree(c->d_tagpr);
   c->d_SI = c->d_SItmp = c->d_split = nullptr;
+  c->d_tagpr = nullptr;
   c->d_info = nullptr;
   c->d_nbr = c->d_sub = nullptr;
   c->d_S = c->d_SN = c->d_SF = nullptr;
   c->d_Snew = c->d_FF = c->d_UF = c->d_GF = c->d_RHS = nullptr;
   c->d_flag = nullptr;
   c->d_list = c->d_bcount = c->d_count = nullptr;
+  c->cap = c->cap_nsub = 0;
   if (c->graph_valid) cudaGraphExecDestroy(c->graph);
   c->graph_valid = 0;
   c->have_mesh = c->have_state = 0;
+}
+
+// the mesh buffers for c->cap cells and c->cap_nsub subface groups
+int alloc_mesh_buffers(ffv_ctx *c) {
+  const int64_t n = c->cap;
+  const size_t nsub = (size_t)c->cap_nsub;
+  if (cudaMalloc(&c->d_info, sizeof(uint32_t) * n) != cudaSuccess ||
+      cudaMalloc(&c->d_nbr, sizeof(int32_t) * 6 * n) != cudaSuccess ||
+      cudaMalloc(&c->d_sub, sizeof(int32_t) * 4 * nsub) != cudaSuccess ||
+      cudaMalloc(&c->d_S, sizeof(double) * c->neq * n) != cudaSuccess ||
+      cudaMalloc(&c->d_SN, sizeof(double) * c->neq * n) != cudaSuccess ||
+      cudaMalloc(&c->d_SF, sizeof(double) * 6 * c->neq * n) != cudaSuccess) {
+    free_mesh_buffers(c);
+    return FFV_ERR_NOMEM;
+  }
+  if (c->p.model == 5) {
+    const int64_t nb = (n + 1023) / 1024;
+    if (cudaMalloc(&c->d_Snew, sizeof(double) * c->neq * n) != cudaSuccess ||
+        cudaMalloc(&c->d_FF, sizeof(double) * 6 * c->neq * n) != cudaSuccess ||
+        cudaMalloc(&c->d_UF, sizeof(double) * 18 * n) != cudaSuccess ||
+        cudaMalloc(&c->d_GF, sizeof(double) * 6 * n) != cudaSuccess ||
+        cudaMalloc(&c->d_RHS, sizeof(double) * c->neq * n) != cudaSuccess ||
+        cudaMalloc(&c->d_flag, n) != cudaSuccess ||
+        cudaMalloc(&c->d_list, sizeof(int32_t) * n) != cudaSuccess ||
+        cudaMalloc(&c->d_bcount, sizeof(int32_t) * nb) != cudaSuccess ||
+        cudaMalloc(&c->d_count, sizeof(int32_t)) != cudaSuccess) {
+      free_mesh_buffers(c);
+      return FFV_ERR_NOMEM;
+    }
+  }
+  return FFV_OK;
 }
 
 unsigned status_to_err(unsigned st) {
@@ -368,47 +406,38 @@ int ffv_set_mesh(ffv_ctx *c, const ffv_mesh *m) {
   if (!c || !m) return FFV_ERR_ARG;
   int rc = ffv_check_frames(m);
   if (rc != FFV_OK) return rc;
-  CK(cudaSetDevice(c->device));
-  CK(cudaStreamSynchronize(c->stream));
-  free_mesh_buffers(c);
-  const int64_t n = m->n;
-  const size_t nsub = (size_t)(m->nsub > 0 ? m->nsub : 1);
   if (c->p.model == 5) {  // symmetry (bc 1) needs m5_hllc.c:56-85's central flux: not built
     for (int s = 0; s < 6; s++)
       if (m->desc.bc[s] == FFV_BC_SYMMETRY) return FFV_ERR_UNSUPPORTED;
   }
-  if (cudaMalloc(&c->d_info, sizeof(uint32_t) * n) != cudaSuccess ||
-      cudaMalloc(&c->d_nbr, sizeof(int32_t) * 6 * n) != cudaSuccess ||
-      cudaMalloc(&c->d_sub, sizeof(int32_t) * 4 * nsub) != cudaSuccess ||
-      cudaMalloc(&c->d_S, sizeof(double) * c->neq * n) != cudaSuccess ||
-      cudaMalloc(&c->d_SN, sizeof(double) * c->neq * n) != cudaSuccess ||
-      cudaMalloc(&c->d_SF, sizeof(double) * 6 * c->neq * n) != cudaSuccess) {
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  const int64_t n_mesh = m->n;
+  const int64_t nsub_mesh = m->nsub > 0 ? m->nsub : 1;
+  if (c->d_info && n_mesh <= c->cap && nsub_mesh <= c->cap_nsub) {
+    // the buffers fit: keep them, drop what belonged to the previous mesh
+    if (c->graph_valid) cudaGraphExecDestroy(c->graph);
+    c->graph_valid = 0;
+    c->have_state = 0;
+  } else {
     free_mesh_buffers(c);
-    return FFV_ERR_NOMEM;
+    // 25 % headroom so that meshes grown by a regrid still fit
+    c->cap = n_mesh + n_mesh / 4 + 1024;
+    c->cap_nsub = nsub_mesh + nsub_mesh / 4 + 1024;
+    rc = alloc_mesh_buffers(c);
+    if (rc != FFV_OK) return rc;
   }
-  if (c->p.model == 5) {
-    const int64_t nb = (n + 1023) / 1024;
-    if (cudaMalloc(&c->d_Snew, sizeof(double) * c->neq * n) != cudaSuccess ||
-        cudaMalloc(&c->d_FF, sizeof(double) * 6 * c->neq * n) != cudaSuccess ||
-        cudaMalloc(&c->d_UF, sizeof(double) * 18 * n) != cudaSuccess ||
-        cudaMalloc(&c->d_GF, sizeof(double) * 6 * n) != cudaSuccess ||
-        cudaMalloc(&c->d_RHS, sizeof(double) * c->neq * n) != cudaSuccess ||
-        cudaMalloc(&c->d_flag, n) != cudaSuccess ||
-        cudaMalloc(&c->d_list, sizeof(int32_t) * n) != cudaSuccess ||
-        cudaMalloc(&c->d_bcount, sizeof(int32_t) * nb) != cudaSuccess ||
-        cudaMalloc(&c->d_count, sizeof(int32_t)) != cudaSuccess) {
-      free_mesh_buffers(c);
-      return FFV_ERR_NOMEM;
-    }
-  }
+  const int64_t n = n_mesh;
   // neighbour slots face-major on the device ([6][n]) for coalesced loads
   int32_t *nbr_t = (int32_t *)malloc(sizeof(int32_t) * 6 * n);
   if (!nbr_t) {
     free_mesh_buffers(c);
     return FFV_ERR_NOMEM;
   }
-  for (int64_t i = 0; i < n; i++)
-    for (int f = 0; f < 6; f++) nbr_t[(int64_t)f * n + i] = m->nbr[6 * i + f];
+  parallel_chunks(n, host_threads(), [&](int, int64_t a, int64_t b) {
+    for (int64_t i = a; i < b; i++)
+      for (int f = 0; f < 6; f++) nbr_t[(int64_t)f * n + i] = m->nbr[6 * i + f];
+  });
   cudaError_t e = cudaMemcpy(c->d_info, m->info, sizeof(uint32_t) * n, cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(c->d_nbr, nbr_t, sizeof(int32_t) * 6 * n, cudaMemcpyHostToDevice);
@@ -642,19 +671,23 @@ int tags_device(ffv_ctx *c, const ffv_mesh *m, const ffv_tag_params *p, int32_t 
   *level_max = lmax;
   CK(cudaSetDevice(c->device));
   const int64_t n = c->n;
-  if (!c->d_split) {
-    if (cudaMalloc(&c->d_SI, sizeof(int32_t) * 2 * n) != cudaSuccess ||
-        cudaMalloc(&c->d_SItmp, sizeof(int32_t) * 2 * n) != cudaSuccess ||
-        cudaMalloc(&c->d_split, sizeof(int32_t) * n) != cudaSuccess) {
+  if (!c->d_split) {  // sized for the mesh buffers' capacity, kept while meshes fit
+    const int64_t cap = c->cap;
+    if (cudaMalloc(&c->d_SI, sizeof(int32_t) * 2 * cap) != cudaSuccess ||
+        cudaMalloc(&c->d_SItmp, sizeof(int32_t) * 2 * cap) != cudaSuccess ||
+        cudaMalloc(&c->d_split, sizeof(int32_t) * cap) != cudaSuccess ||
+        cudaMalloc(&c->d_tagpr, sizeof(double) * 2 * cap) != cudaSuccess) {
       cudaFree(c->d_SI);
       cudaFree(c->d_SItmp);
       cudaFree(c->d_split);
+      cudaFree(c->d_tagpr);
       c->d_SI = c->d_SItmp = c->d_split = nullptr;
+      c->d_tagpr = nullptr;
       return FFV_ERR_NOMEM;
     }
   }
   if (c->p.model == 5) {
-    ffv_m5_tags(c->dm, c->m5, t, c->d_S, c->d_SI, c->d_SItmp, c->d_split, c->stream);
+    ffv_m5_tags(c->dm, c->m5, t, c->d_S, c->d_SI, c->d_SItmp, c->d_split, c->d_tagpr, c->stream);
   } else {
     ffv_m0_tags(c->dm, c->p.gamma[0], c->p.pinf[0], t, c->d_S, c->d_split, c->stream);
     CK(cudaMemsetAsync(c->d_SI, 0, sizeof(int32_t) * 2 * n, c->stream));

@@ -82,8 +82,9 @@ struct ffv_m5_tagc {
   double thr_prs, thr_rho, thr_vel;
 };
 // SI [2][n] (interface layers), SItmp scratch of the same size, split [n]
+// pr: scratch [2][n] doubles (each cell's mixture pressure and density, made once)
 void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, const double *S,
-                 int32_t *SI, int32_t *SItmp, int32_t *split, cudaStream_t st);
+                 int32_t *SI, int32_t *SItmp, int32_t *split, double *pr, cudaStream_t st);
 
 // exported per-leaf fields, F [nf][n] double (ffv_export_fields)
 void ffv_m5_export_fields(int64_t n, const M5Consts &k, const double *S, double *F,

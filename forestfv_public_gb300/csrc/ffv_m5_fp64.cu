@@ -1392,45 +1392,52 @@ __device__ __forceinline__ double rel_jump(double x_cur, double x_nb) {
   return 0.0;
 }
 
+// each cell's alpha-weighted pressure sum_k alpha_k p_k and density, from the reference's cell
+// primitives (make_sol of the cell state): computed once per cell here, read by every
+// neighbour's criterion below (the same doubles the per-neighbour evaluation gave)
+template <int N>
+__global__ void __launch_bounds__(128) m5_tag_prims(int64_t n, M5Consts k,
+                                                    const double *__restrict__ S,
+                                                    double *__restrict__ pr) {
+  using C = K5<N>;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double s[C::NEQ];
+  load_state<N>(S, n, c, s);
+  Sol<N> q;
+  make_sol<N>(k, s, s, false, q);
+  double p = 0.0;
+#pragma unroll
+  for (int iv = 0; iv < N; ++iv) p += q.avf[iv] * q.p[iv];
+  pr[c] = p;
+  pr[n + c] = q.r;
+}
+
 // criterionsplt.c:3-140 per cell: the uniform level, the gradient criterion over every
 // sub-neighbour and the interface layers
-template <int N>
-__global__ void __launch_bounds__(128) m5_tag_split(ffv_dmesh m, M5Consts k, ffv_m5_tagc t,
-                                                    const double *__restrict__ S,
+__global__ void __launch_bounds__(128) m5_tag_split(ffv_dmesh m, ffv_m5_tagc t,
+                                                    const double *__restrict__ pr,
                                                     const int32_t *__restrict__ SI,
                                                     int32_t *__restrict__ split) {
-  using C = K5<N>;
   const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= m.n) return;
   int level = 1;
   if (t.uniform == 1) level = level > t.lvl_uniform ? level : t.lvl_uniform;
   if (t.prs == 1 || t.rho == 1 || t.vel == 1) {
     const uint32_t info = m.info[c];
-    double s[C::NEQ];
-    load_state<N>(S, m.n, c, s);
-    Sol<N> L;
-    make_sol<N>(k, s, s, false, L);
-    double pL = 0.0;
-#pragma unroll
-    for (int iv = 0; iv < N; ++iv) pL += L.avf[iv] * L.p[iv];
+    const double pL = pr[c], rL = pr[m.n + c];
     double gp = 0.0, gr = 0.0, gv = 0.0;
     for (int f = 0; f < 6; f++) {
       int64_t nb[4];
       const int cnt = face_neighbours(m, c, info, f, nb);
       for (int q = 0; q < cnt; q++) {
-        load_state<N>(S, m.n, nb[q], s);
-        Sol<N> R;
-        make_sol<N>(k, s, s, false, R);
         if (t.prs == 1) {
-          double pR = 0.0;
-#pragma unroll
-          for (int iv = 0; iv < N; ++iv) pR += R.avf[iv] * R.p[iv];
-          const double g = rel_jump(pL, pR);
+          const double g = rel_jump(pL, pr[nb[q]]);
           gp = (g > gp) ? g : gp;
         }
         double grho = 0.0;
         if (t.rho == 1) {
-          grho = rel_jump(L.r, R.r);
+          grho = rel_jump(rL, pr[m.n + nb[q]]);
           gr = (grho > gr) ? grho : gr;
         }
         // the reference's velocity criterion takes the density jump (criterionsplt.c:120)
@@ -1524,7 +1531,7 @@ void ffv_m5_export_fields(int64_t n, const M5Consts &k, const double *S, double 
 }
 
 void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, const double *S,
-                 int32_t *SI, int32_t *SItmp, int32_t *split, cudaStream_t st) {
+                 int32_t *SI, int32_t *SItmp, int32_t *split, double *pr, cudaStream_t st) {
   const unsigned gc = (unsigned)((m.n + 127) / 128);
   if (t.inter0 != 0) {
     if (k.nmat == 2) m5_si_first<2><<<gc, 128, 0, st>>>(m, k, S, SI);
@@ -1536,8 +1543,11 @@ void ffv_m5_tags(const ffv_dmesh &m, const M5Consts &k, const ffv_m5_tagc &t, co
   } else {
     cudaMemsetAsync(SI, 0, sizeof(int32_t) * 2 * m.n, st);
   }
-  if (k.nmat == 2) m5_tag_split<2><<<gc, 128, 0, st>>>(m, k, t, S, SI, split);
-  else m5_tag_split<3><<<gc, 128, 0, st>>>(m, k, t, S, SI, split);
+  if (t.prs == 1 || t.rho == 1 || t.vel == 1) {
+    if (k.nmat == 2) m5_tag_prims<2><<<gc, 128, 0, st>>>(m.n, k, S, pr);
+    else m5_tag_prims<3><<<gc, 128, 0, st>>>(m.n, k, S, pr);
+  }
+  m5_tag_split<<<gc, 128, 0, st>>>(m, t, pr, SI, split);
 }
 
 void ffv_m5_cfl(const ffv_dmesh &m, const ffv_geom &g, const M5Consts &k, const double *S,
