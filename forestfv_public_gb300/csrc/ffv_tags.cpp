@@ -60,20 +60,47 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
     return mx - split[c] > 1 ? mx - 1 : split[c];
   };
   // A sweep updates split in place in leaf order, each leaf seeing its predecessors' new
-  // values.  It runs as a worklist with the same result: all leaves are first evaluated on
+  // values.  It runs as a worklist with the same result: the leaves are first evaluated on
   // the sweep's input in parallel, and those whose value would change are visited in leaf
   // order; when a visited leaf changes, the later leaves that read its value (its sibling
   // group for the coarsening rule, its face neighbours for the 2:1 rule) join the worklist.
   // A leaf never on the list sees, when the sweep reaches it, exactly the inputs of the
   // parallel evaluation, so its value does not change -- as in the full sweep.  Earlier
   // leaves that read a changed value are not revisited in this sweep (the full sweep has
-  // passed them too); the next pass's parallel evaluation finds them.
-  std::vector<uint8_t> queued(n, 0);
-  auto sweep = [&](auto rule, bool sibling_deps) -> bool {
+  // passed them too); the next pass's evaluation finds them.  That evaluation visits only
+  // "dirty" leaves: all at first, afterwards those one of whose inputs (their own value, a
+  // sibling's or a face neighbour's, per rule) changed since they were last evaluated -- a
+  // leaf found unchanged stays unchanged until then.
+  std::vector<uint8_t> queued(n, 0), dirty1(n, 1), dirty2(n, 1);
+  auto mark_deps = [&](int64_t c, bool siblings, auto &&fn) {
+    fn(c);
+    if (siblings) {
+      const int64_t g = group[c];
+      if (g >= 0)
+        for (int64_t q = g; q < g + 8; q++) fn(q);
+    } else {
+      const uint32_t info = m->info[c];
+      for (int f = 0; f < 6; f++) {
+        const uint32_t kind = ffv_face_kind(info, f);
+        if (kind & FFV_FK_BC) continue;
+        const int32_t s = m->nbr[6 * c + f];
+        if (kind == FFV_FK_FINER) {
+          for (int q = 0; q < 4; q++) fn(m->sub[4 * (int64_t)s + q]);
+        } else {
+          fn(s);
+        }
+      }
+    }
+  };
+  auto sweep = [&](auto rule, bool sibling_deps, std::vector<uint8_t> &dirty,
+                   std::vector<uint8_t> &dirty_other) -> bool {
     std::vector<std::vector<int64_t>> found(nth);
     parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
-      for (int64_t c = a; c < b; c++)
+      for (int64_t c = a; c < b; c++) {
+        if (!dirty[c]) continue;
+        dirty[c] = 0;
         if (rule(c) != split[c]) found[t].push_back(c);
+      }
     });
     std::priority_queue<int64_t, std::vector<int64_t>, std::greater<int64_t>> work;
     for (auto &v : found)
@@ -82,13 +109,6 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
         queued[c] = 1;
       }
     if (work.empty()) return false;
-    bool changed = false;
-    auto push_later = [&](int64_t d, int64_t cur) {
-      if (d > cur && !queued[d]) {
-        queued[d] = 1;
-        work.push(d);
-      }
-    };
     while (!work.empty()) {
       const int64_t c = work.top();
       work.pop();
@@ -96,32 +116,28 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
       const int32_t v = rule(c);
       if (v == split[c]) continue;
       split[c] = v;
-      changed = true;
-      if (sibling_deps) {
-        const int64_t g = group[c];
-        if (g >= 0)
-          for (int64_t q = g; q < g + 8; q++) push_later(q, c);
-      } else {
-        const uint32_t info = m->info[c];
-        for (int f = 0; f < 6; f++) {
-          const uint32_t kind = ffv_face_kind(info, f);
-          if (kind & FFV_FK_BC) continue;
-          const int32_t s = m->nbr[6 * c + f];
-          if (kind == FFV_FK_FINER) {
-            for (int q = 0; q < 4; q++) push_later(m->sub[4 * (int64_t)s + q], c);
-          } else {
-            push_later(s, c);
+      // this rule's readers of split[c]: later ones in this sweep, earlier ones (and c
+      // itself, whose rule reads its own value) in the next pass
+      mark_deps(c, sibling_deps, [&](int64_t d) {
+        if (d > c) {
+          if (!queued[d]) {
+            queued[d] = 1;
+            work.push(d);
           }
+        } else {
+          dirty[d] = 1;
         }
-      }
+      });
+      // the other rule's readers: at its next sweep
+      mark_deps(c, !sibling_deps, [&](int64_t d) { dirty_other[d] = 1; });
     }
-    return changed;
+    return true;
   };
   // A pass is a function of `split` alone: once one changes nothing, every later pass
   // would see the same input and change nothing either, so the passes end there.
   for (int32_t pass = 0; pass < level_max + 1; pass++) {
-    const bool c1 = sweep(rule1, true);
-    const bool c2 = sweep(rule2, false);
+    const bool c1 = sweep(rule1, true, dirty1, dirty2);
+    const bool c2 = sweep(rule2, false, dirty2, dirty1);
     if (!c1 && !c2) break;
   }
   return FFV_OK;

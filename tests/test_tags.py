@@ -46,3 +46,56 @@ def test_smoothing_is_two_to_one():
                 for q in nb[c, f]:
                     if q >= 0:
                         assert split[q] - split[c] <= 1
+
+
+def _smooth_sequential(m, lmax, split):
+    """criterionsmth.c:3-58 restated plainly: LEVEL + 1 passes of the two in-place sweeps in
+    leaf order (coarsen only with all eight sibling leaves, refine by one; at most one level
+    below any face neighbour)."""
+    split = split.copy()
+    n, lev = m.n, m.level
+    c_ijk, t_ijk = m.cell_ijk, m.tree_ijk
+    kid = ((c_ijk[:, 0] & 1) << 1) | (c_ijk[:, 1] & 1) | ((c_ijk[:, 2] & 1) << 2)
+    group = np.full(n, -1)
+    for c in range(n):
+        s = c - kid[c]
+        if lev[c] > 1 and s >= 0 and s + 8 <= n and all(
+                lev[s + q] == lev[c] and kid[s + q] == q and (t_ijk[s + q] == t_ijk[c]).all()
+                and ((c_ijk[s + q] >> 1) == (c_ijk[c] >> 1)).all() for q in range(8)):
+            group[c] = s
+    e = m.export()
+    nbrs = [[int(e["nb"][c, f, q]) for f in range(6) for q in range(int(e["nn"][c, f]))]
+            for c in range(n)]
+    for _ in range(lmax + 1):
+        for c in range(n):
+            l = lev[c]
+            if l > 1:
+                g = group[c]
+                imerge = sum(1 for q in range(g, g + 8) if split[q] < lev[q]) if g >= 0 else 0
+                if imerge == 8:
+                    split[c] = l - 1
+                elif l > split[c]:
+                    split[c] = l
+            if l < split[c]:
+                split[c] = l + 1
+        for c in range(n):
+            mx = max([1] + [split[d] for d in nbrs[c]])
+            if mx - split[c] > 1:
+                split[c] = mx - 1
+    return split
+
+
+@pytest.mark.parametrize("seed", [3, 4, 5])
+def test_smoothing_equals_sequential_sweeps(seed, built_lib):
+    """The worklist smoothing (parallel evaluation of dirty leaves, in-place visits in leaf
+    order) against the plain sequential sweeps, on random targets of an AMR forest."""
+    from forestfv_public_gb300 import Mesh
+    from forestfv_public_gb300.solver import tags_smooth
+    from forestfv_public_gb300.workloads import refine_to_target
+    rng = np.random.default_rng(seed)
+    leaves = refine_to_target((2, 2, 2), 2, 4, lambda c, h: np.where(
+        c[:, 0] < 0.25, 4, np.where(c[:, 0] < 0.5, 3, 2)))
+    m = Mesh((2, 2, 2), leaves)
+    lmax = 6
+    split = np.clip(m.level + rng.integers(-2, 3, m.n), 1, lmax).astype(np.int32)
+    assert np.array_equal(tags_smooth(m, lmax, split), _smooth_sequential(m, lmax, split))
