@@ -14,7 +14,9 @@ runs as a judge on the device (ffv_tags_missed): when no cell is below its targe
 the regrid is skipped, otherwise -- and after `max_skips` skipped regrids in a row, so that
 the mesh can coarsen -- a regrid runs.  Its target is the criterion's raw level, raised on
 the marked cells to the level the gradient criteria assign (`pre_level`), then smoothed
-(criterionsmth); later rounds carry the marks to the new leaves (children inherit them).  Any cell the
+(criterionsmth); later rounds carry the marks to the new leaves (children inherit them), and
+the rounds end as soon as every leaf has reached the round's target (what the criterion
+wants on the new state, the next judge finds).  Any cell the
 criterion flags is refined whether or not the network marked it: the criterion is the
 fallback.
 """
@@ -140,6 +142,12 @@ class AdaptiveRun:
             _, src = s.adapt(tgt, with_src=True)
             marks = carry_marks(src, marks)
             rounds += 1
+            # every leaf at (or, for a sibling group that could not merge, above) its
+            # target: no further round, whatever the criterion wants on the new state the
+            # next judge finds
+            from_leaf = src >= 0
+            if not np.any(tgt[src[from_leaf]] > s.mesh.level[from_leaf]):
+                break
         self.marks = None
         return rounds
 
