@@ -19,26 +19,37 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   if (!m || !split || level_max < 0) return FFV_ERR_ARG;
   const int64_t n = m->n;
   const int nth = host_threads();
-  // complete groups of eight sibling leaves (first cell, or -1)
-  std::vector<int64_t> group(n);
-  parallel_chunks(n, nth, [&](int, int64_t a, int64_t b) {
-    for (int64_t c = a; c < b; c++) group[c] = ffv_sibling_group(m, c);
-  });
   auto level = [&](int64_t c) { return (int32_t)ffv_info_level(m->info[c]); };
-  // criterionsmth.c:14-33: a leaf coarsens only with all eight siblings, refines by one
+  // a leaf's complete group of eight sibling leaves (first leaf, or -1), looked up once and
+  // remembered as one byte (0 not looked up, 1 in a complete group, 2 not); each entry is
+  // written only by the thread that evaluates its own leaf
+  std::vector<uint8_t> gknown(n, 0);
+  auto group_of = [&](int64_t c) -> int64_t {
+    const uint8_t f = gknown[c];
+    if (f == 0) {
+      const int64_t g = ffv_sibling_group(m, c);
+      gknown[c] = g >= 0 ? 1 : 2;
+      return g;
+    }
+    if (f == 2) return -1;
+    const int32_t *x = m->cell_ijk + 3 * c;
+    return c - (((x[0] & 1) << 1) | (x[1] & 1) | ((x[2] & 1) << 2));
+  };
+  // criterionsmth.c:14-33: a leaf coarsens only with all eight siblings, refines by one.
+  // A leaf whose target is not below its level counts itself out of the eight, so its
+  // sibling group is only looked up for targets below the level.
   auto rule1 = [&](int64_t c) {
     const int32_t l = level(c);
     int32_t v = split[c];
-    if (l > 1) {
+    if (l > 1 && v < l) {
       // only leaf children count (criterionsmth.c:19-21): a group with a refined sibling
       // cannot reach eight
-      const int64_t g = group[c];
+      const int64_t g = group_of(c);
       int imerge = 0;
       if (g >= 0)
         for (int64_t q = g; q < g + 8; q++)
           if (split[q] < level(q)) imerge++;
-      if (imerge == 8) v = l - 1;
-      else if (l > v) v = l;
+      v = imerge == 8 ? l - 1 : l;
     }
     if (l < v) v = l + 1;
     return v;
@@ -72,10 +83,14 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   // sibling's or a face neighbour's, per rule) changed since they were last evaluated -- a
   // leaf found unchanged stays unchanged until then.
   std::vector<uint8_t> queued(n, 0), dirty1(n, 1), dirty2(n, 1);
-  auto mark_deps = [&](int64_t c, bool siblings, auto &&fn) {
+  // the readers of split[c]: c itself and, for the coarsening rule, its siblings (which
+  // read only whether split[c] is below the level: `flipped`), for the 2:1 rule its face
+  // neighbours
+  auto mark_deps = [&](int64_t c, bool siblings, bool flipped, auto &&fn) {
     fn(c);
     if (siblings) {
-      const int64_t g = group[c];
+      if (!flipped) return;
+      const int64_t g = group_of(c);
       if (g >= 0)
         for (int64_t q = g; q < g + 8; q++) fn(q);
     } else {
@@ -115,10 +130,12 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
       queued[c] = 0;
       const int32_t v = rule(c);
       if (v == split[c]) continue;
+      const int32_t lc = level(c);
+      const bool flipped = (split[c] < lc) != (v < lc);
       split[c] = v;
       // this rule's readers of split[c]: later ones in this sweep, earlier ones (and c
       // itself, whose rule reads its own value) in the next pass
-      mark_deps(c, sibling_deps, [&](int64_t d) {
+      mark_deps(c, sibling_deps, flipped, [&](int64_t d) {
         if (d > c) {
           if (!queued[d]) {
             queued[d] = 1;
@@ -129,7 +146,7 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
         }
       });
       // the other rule's readers: at its next sweep
-      mark_deps(c, !sibling_deps, [&](int64_t d) { dirty_other[d] = 1; });
+      mark_deps(c, !sibling_deps, flipped, [&](int64_t d) { dirty_other[d] = 1; });
     }
     return true;
   };
