@@ -29,24 +29,28 @@ namespace {
 constexpr int kDepth = FFV_MAX_LEVEL - 1;  // Morton digits below the tree at the finest level
 
 struct Leaves {
-  std::vector<int32_t> tij, lev, cij;  // new leaves in leaf order
-  std::vector<int64_t> src;            // old leaf copied or split (>= 0), -1 - j merged from j..j+7
-  std::vector<int64_t> old2new;        // kept old leaves' new index, else -1
-  std::vector<uint8_t> what;           // per old leaf: 0 absorbed, 1 kept, 2 merged parent, 8 split
+  int32_t *tij = nullptr, *cij = nullptr;  // new leaves in leaf order (the new mesh's arrays)
+  std::vector<int32_t> lev;
+  std::vector<int64_t> src;      // old leaf copied or split (>= 0), -1 - j merged from j..j+7
+  std::vector<int32_t> old2new;  // kept old leaves' new index, else -1
+  std::vector<uint8_t> what;     // per old leaf: 0 absorbed, 1 kept, 2 merged parent, 8 split
+  std::vector<int64_t> tsum;     // new leaves before each chunk of old leaves
+  int64_t nn = 0;
 };
 
-// the pass's new leaves: a per-old-leaf count, a prefix sum and a parallel fill, in the order
-// one sweep in leaf order emits them
-int sweep_leaves(const ffv_mesh *m, const int32_t *split, int nth, Leaves &L) {
+// the pass's new leaves, counted: a per-old-leaf count and a prefix sum (a leaf whose
+// target is not below its level cannot be part of a merge: no group lookup)
+int count_leaves(const ffv_mesh *m, const int32_t *split, int nth, Leaves &L) {
   const int64_t n = m->n;
-  L.what.assign(n, 0);
-  std::vector<int64_t> tsum(nth + 1, 0);
+  L.what.resize(n);
+  std::vector<int64_t> &tsum = L.tsum;
+  tsum.assign(nth + 1, 0);
   std::vector<char> bad(nth, 0);
   parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
     int64_t acc = 0;
     for (int64_t c = a; c < b; c++) {
       const int l = ffv_info_level(m->info[c]);
-      const int64_t g = l > 1 ? ffv_sibling_group(m, c) : -1;
+      const int64_t g = (l > 1 && split[c] < l) ? ffv_sibling_group(m, c) : -1;
       bool merge = g >= 0;
       for (int q = 0; q < 8 && merge; q++) merge = split[g + q] < l;
       uint8_t k;
@@ -61,16 +65,22 @@ int sweep_leaves(const ffv_mesh *m, const int32_t *split, int nth, Leaves &L) {
   });
   if (std::any_of(bad.begin(), bad.end(), [](char x) { return x != 0; })) return FFV_ERR_TABLE;
   for (int t = 0; t < nth; t++) tsum[t + 1] += tsum[t];
-  const int64_t nn = tsum[nth];
-  L.tij.resize(3 * nn);
+  L.nn = tsum[nth];
+  return FFV_OK;
+}
+
+// the new leaves written in the order one sweep in leaf order emits them, into L.tij / L.cij
+void fill_leaves(const ffv_mesh *m, int nth, Leaves &L) {
+  const int64_t n = m->n, nn = L.nn;
+  const std::vector<int64_t> &tsum = L.tsum;
   L.lev.resize(nn);
-  L.cij.resize(3 * nn);
   L.src.resize(nn);
-  L.old2new.assign(n, -1);
+  L.old2new.resize(n);
   parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
     int64_t o = tsum[t];
     for (int64_t c = a; c < b; c++) {
       const uint8_t k = L.what[c];
+      L.old2new[c] = k == 1 ? (int32_t)o : -1;
       if (k == 0) continue;
       const int l = ffv_info_level(m->info[c]);
       const int32_t *tr = m->tree_ijk + 3 * c, *x = m->cell_ijk + 3 * c;
@@ -98,12 +108,10 @@ int sweep_leaves(const ffv_mesh *m, const int32_t *split, int nth, Leaves &L) {
         }
         L.lev[o] = l;
         L.src[o] = c;
-        L.old2new[c] = o;
         o++;
       }
     }
   });
-  return FFV_OK;
 }
 
 // rank of each tree in Morton order of its coordinates, by linear index (i * ny + j) * nz + k
@@ -128,13 +136,34 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
   *out = nullptr;
   const int nth = host_threads();
   Leaves L;
-  int rc = sweep_leaves(m, split, nth, L);
+  int rc = count_leaves(m, split, nth, L);
   if (rc != FFV_OK) return rc;
-  const int64_t nn = (int64_t)L.lev.size();
+  const int64_t nn = L.nn;
   if (nn > INT32_MAX) return FFV_ERR_TABLE;
+  ffv_mesh *nm = new (std::nothrow) ffv_mesh();
+  if (!nm) return FFV_ERR_NOMEM;
+  memset(nm, 0, sizeof(*nm));
+  nm->desc = m->desc;
+  nm->n = nn;
+  memcpy(nm->frame, m->frame, sizeof(m->frame));
+  memcpy(nm->geom, m->geom, sizeof(m->geom));
+  nm->info = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nn ? nn : 1));
+  nm->nbr = (int32_t *)malloc(sizeof(int32_t) * 6 * (size_t)(nn ? nn : 1));
+  nm->tree_ijk = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(nn ? nn : 1));
+  nm->cell_ijk = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(nn ? nn : 1));
+  if (!nm->info || !nm->nbr || !nm->tree_ijk || !nm->cell_ijk) {
+    ffv_mesh_free(nm);
+    return FFV_ERR_NOMEM;
+  }
+  L.tij = nm->tree_ijk;
+  L.cij = nm->cell_ijk;
+  fill_leaves(m, nth, L);
   const int32_t *NT = m->desc.ntrees;
   const std::vector<uint64_t> rank = tree_ranks(NT);
-  if (rank.size() >= (1ull << (64 - 3 * kDepth))) return FFV_ERR_TABLE;
+  if (rank.size() >= (1ull << (64 - 3 * kDepth))) {
+    ffv_mesh_free(nm);
+    return FFV_ERR_TABLE;
+  }
   auto lin = [&](int64_t i, int64_t j, int64_t k) { return (i * NT[1] + j) * NT[2] + k; };
   // the key of the first point of the level-l cell at global coordinates g (level l)
   auto point_key = [&](int l, const int64_t g[3]) {
@@ -159,8 +188,10 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
   parallel_chunks(nn > 0 ? nn - 1 : 0, nth, [&](int t, int64_t a, int64_t b) {
     for (int64_t j = a; j < b && !unsorted[t]; j++) unsorted[t] = !(key[j] < key[j + 1]);
   });
-  if (std::any_of(unsorted.begin(), unsorted.end(), [](char x) { return x != 0; }))
+  if (std::any_of(unsorted.begin(), unsorted.end(), [](char x) { return x != 0; })) {
+    ffv_mesh_free(nm);
     return FFV_ERR_TABLE;
+  }
   auto find = [&](uint64_t pk) {
     return (int64_t)(std::upper_bound(key.begin(), key.end(), pk) - key.begin()) - 1;
   };
@@ -186,23 +217,6 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
     }
   });
 
-  ffv_mesh *nm = new (std::nothrow) ffv_mesh();
-  if (!nm) return FFV_ERR_NOMEM;
-  memset(nm, 0, sizeof(*nm));
-  nm->desc = m->desc;
-  nm->n = nn;
-  memcpy(nm->frame, m->frame, sizeof(m->frame));
-  memcpy(nm->geom, m->geom, sizeof(m->geom));
-  nm->info = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)(nn ? nn : 1));
-  nm->nbr = (int32_t *)malloc(sizeof(int32_t) * 6 * (size_t)(nn ? nn : 1));
-  nm->tree_ijk = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(nn ? nn : 1));
-  nm->cell_ijk = (int32_t *)malloc(sizeof(int32_t) * 3 * (size_t)(nn ? nn : 1));
-  if (!nm->info || !nm->nbr || !nm->tree_ijk || !nm->cell_ijk) {
-    ffv_mesh_free(nm);
-    return FFV_ERR_NOMEM;
-  }
-  memcpy(nm->tree_ijk, L.tij.data(), sizeof(int32_t) * 3 * nn);
-  memcpy(nm->cell_ijk, L.cij.data(), sizeof(int32_t) * 3 * nn);
 
   const int64_t chunk = (nn + nth - 1) / (nth ? nth : 1);
   std::vector<std::vector<int32_t>> csub(nth);
