@@ -403,30 +403,6 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
   return st;
 }
 
-// avf_limit.c:3-21 on a state vector
-template <int N>
-__device__ __forceinline__ void avf_limit_d(const M5Consts &k, double *S) {
-  using C = K5<N>;
-  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
-  double sum = 0.0;
-#pragma unroll
-  for (int v = 0; v < N - 1; ++v) {
-    double a = S[C::i3 + v];
-    if (a <= lo) a = lo;
-    else if (a >= hi) a = hi;
-    S[C::i3 + v] = a;
-    sum += a;
-  }
-  if (sum > hi) {
-    const double dif = sum - hi;
-#pragma unroll
-    for (int j = 0; j < N - 1; ++j) {
-      const double a = S[C::i3 + j];
-      S[C::i3 + j] = a - (a / sum) * dif;
-    }
-  }
-}
-
 // face record of a state V (FP64): conserved variables, the volume fractions as the FP64
 // form's make_sol clamps them, and each material's pressure recovered in FP64
 template <int N>
@@ -598,9 +574,9 @@ __device__ void crit_across_df(const M5Consts &k, const ffv_dmesh &m, const floa
   avf_limit_df<N>(k, X);
 }
 
-// vf_limit_relax_d in double-float: the N-1 fractions clamped (else-if or two ifs as the
-// reference's two call sites have it), renormalised when their sum reaches 1 - lo, the last
-// fraction 1 - sum
+// the volume-fraction limits of m5_relaxationvec.c in double-float: the N-1 fractions
+// clamped (else-if or two ifs as the reference's two call sites have it), renormalised when
+// their sum reaches 1 - lo, the last fraction 1 - sum
 template <int N>
 __device__ __forceinline__ void vf_limit_relax_df(const M5Consts &k, df *avf, bool elseif) {
   df sum = df_make(0.0f);
