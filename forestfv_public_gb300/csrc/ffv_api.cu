@@ -406,10 +406,6 @@ int ffv_set_mesh(ffv_ctx *c, const ffv_mesh *m) {
   if (!c || !m) return FFV_ERR_ARG;
   int rc = ffv_check_frames(m);
   if (rc != FFV_OK) return rc;
-  if (c->p.model == 5) {  // symmetry (bc 1) needs m5_hllc.c:56-85's central flux: not built
-    for (int s = 0; s < 6; s++)
-      if (m->desc.bc[s] == FFV_BC_SYMMETRY) return FFV_ERR_UNSUPPORTED;
-  }
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->stream));
   const int64_t n_mesh = m->n;

@@ -196,7 +196,7 @@ __device__ __forceinline__ float cell_phi0_f(const M5Consts &k, const float *__r
 template <int F, int N>
 __device__ __forceinline__ void ghost_f(const SolF<N> &L, int bc, SolF<N> &R) {
   R = L;
-  if (bc == 4 || bc == 5) {
+  if (bc == 1 || bc == 4 || bc == 5) {
     const float v3[3] = {L.u, L.v, L.w};
     const float ul = loc<F, 0>(v3), vl = loc<F, 1>(v3), wl = loc<F, 2>(v3);
     const float ur = -ul, vr = bc == 5 ? -vl : vl, wr = bc == 5 ? -wl : wl;
@@ -325,6 +325,13 @@ __device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, NCf<N> &nc, float
     for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
 #pragma unroll
     for (int q = 0; q < 9; q++) nc.A[q] = gfm ? s.A[q] : -s.A[q];
+  } else if (flag == 4) {  // symmetry face (m5_flux.c:58-66): the velocity is the caller's
+#pragma unroll
+    for (int v = 0; v < N - 1; ++v) nc.avf[v] = s.avf[v];
+#pragma unroll
+    for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
+#pragma unroll
+    for (int q = 0; q < 9; q++) nc.A[q] = s.A[q];
   }
   const float ua = nc.unc[a];
 #pragma unroll
@@ -401,6 +408,26 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
 #pragma unroll
   for (int d = 0; d < 3; d++) unc[d] = nc.unc[d];
   return st;
+}
+
+// m5_hllc.c:56-85 in FP32, a symmetry face: the mean of the physical fluxes of the cell's own
+// state and of its mirror image, advected terms moving with the mean velocity, no HLLC part
+template <int F, int N>
+__device__ void symmetry_acc_f(const SolF<N> &Lc, float Area, float *ff, float unc[3]) {
+  using C = K5<N>;
+  SolF<N> Rc;
+  ghost_f<F, N>(Lc, 1, Rc);
+  NCf<N> nc;
+  nc.unc[0] = 0.5f * (Lc.u + Rc.u);
+  nc.unc[1] = 0.5f * (Lc.v + Rc.v);
+  nc.unc[2] = 0.5f * (Lc.w + Rc.w);
+  float FL[C::NEQ], FR[C::NEQ];
+  flux_n_f<F>(Lc, 4, false, nc, FL);
+  flux_n_f<F>(Rc, 4, false, nc, FR);
+#pragma unroll
+  for (int iv = 0; iv < C::NEQ; ++iv) ff[iv] += Area * ((0.5f * FL[iv]) + (0.5f * FR[iv]));
+#pragma unroll
+  for (int d = 0; d < 3; d++) unc[d] = nc.unc[d];
 }
 
 // face record of a state V (FP64): conserved variables, the volume fractions as the FP64
@@ -973,6 +1000,12 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
   }
   float U[RL::SIZE];
   SolF<N> L, R;
+  if (kind == (FFV_FK_BC | FFV_BC_SYMMETRY)) {  // the cell's own state (m5_hllc.c:59-63)
+    record_of_cell<N>(k, S, m.n, c, U);
+    make_sol_f<N>(k, U, 0.0f, L);
+    symmetry_acc_f<F, N>(L, (float)g.area[l], ff, uf);
+    return;
+  }
   if (k.order == 2) load_record<N>(SF, m.n, F, c, U);
   else record_of_cell<N>(k, S, m.n, c, U);
   make_sol_f<N>(k, U, Sf ? cell_phi0_f<N>(k, Sf, m.n, c) : (float)cell_phi0<N>(k, S, m.n, c), L);

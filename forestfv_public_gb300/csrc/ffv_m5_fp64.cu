@@ -185,11 +185,11 @@ __device__ void make_sol(const M5Consts &k, const double *U, const double *Sc, b
   s.c2 = c2;
 }
 
-// m5_bc.c / bc_reflective.c / bc_wall.c: ghost velocity
+// m5_bc.c (m5_bc_symmetry) / bc_reflective.c / bc_wall.c: ghost velocity
 template <int F, int N>
 __device__ __forceinline__ void ghost(const Sol<N> &L, int bc, Sol<N> &R) {
   R = L;
-  if (bc == 4 || bc == 5) {
+  if (bc == 1 || bc == 4 || bc == 5) {
     const double v3[3] = {L.u, L.v, L.w};
     const double ul = loc<F, 0>(v3), vl = loc<F, 1>(v3), wl = loc<F, 2>(v3);
     const double ur = -ul, vr = bc == 5 ? -vl : vl, wr = bc == 5 ? -wl : wl;
@@ -323,6 +323,13 @@ __device__ void flux_n(const Sol<N> &s, int flag, bool gfm, NC<N> &nc, double *F
     for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
 #pragma unroll
     for (int q = 0; q < 9; q++) nc.A[q] = gfm ? s.A[q] : -s.A[q];
+  } else if (flag == 4) {  // symmetry face (m5_flux.c:58-66): the velocity is the caller's
+#pragma unroll
+    for (int v = 0; v < N - 1; ++v) nc.avf[v] = s.avf[v];
+#pragma unroll
+    for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
+#pragma unroll
+    for (int q = 0; q < 9; q++) nc.A[q] = s.A[q];
   }
   const double ua = nc.unc[a];
 #pragma unroll
@@ -404,6 +411,28 @@ __device__ unsigned hllc_acc(const M5Consts &k, Sol<N> L, Sol<N> R, int bc, bool
 #pragma unroll
   for (int d = 0; d < 3; d++) unc[d] = nc.unc[d];
   return st;
+}
+
+// m5_hllc.c:56-85, a symmetry face (bc 1): the mean of the physical fluxes of the cell's own
+// state (m5_facevalues.c, not the reconstructed face state) and of its mirror image
+// (m5_bc_symmetry: normal velocity reversed), the advected volume fractions, energies and
+// deformation moving with the mean velocity, no HLLC part; accumulated as m5_residual.c:155-165
+template <int F, int N>
+__device__ void symmetry_acc(const Sol<N> &Lc, double Area, double *ff, double unc[3]) {
+  using C = K5<N>;
+  Sol<N> Rc;
+  ghost<F, N>(Lc, 1, Rc);
+  NC<N> nc;
+  nc.unc[0] = 0.5 * (Lc.u + Rc.u);
+  nc.unc[1] = 0.5 * (Lc.v + Rc.v);
+  nc.unc[2] = 0.5 * (Lc.w + Rc.w);
+  double FL[C::NEQ], FR[C::NEQ];
+  flux_n<F>(Lc, 4, false, nc, FL);
+  flux_n<F>(Rc, 4, false, nc, FR);
+#pragma unroll
+  for (int iv = 0; iv < C::NEQ; ++iv) ff[iv] += (Area) * ((0.5 * FL[iv]) + (0.5 * FR[iv]));
+#pragma unroll
+  for (int d = 0; d < 3; d++) unc[d] = nc.unc[d];
 }
 
 // ------------------------------------------------------------ relaxation (m5_relaxationvec.c)
@@ -764,6 +793,13 @@ __device__ void face_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts 
     // it (face F^1 of the neighbour) and m5_cell_update takes the negative, as the
     // reference's flux reuse does (m5_residual.c:80-99); no ghost-fluid flag here
     owner = false;
+    return;
+  }
+  if (kind == (FFV_FK_BC | FFV_BC_SYMMETRY)) {
+    // the cell's own state, not the face state; the HLLC flux the reference computes first
+    // for this face is discarded (m5_hllc.c:59-63)
+    make_sol<N>(k, Sc, Sc, false, L);
+    symmetry_acc<F, N>(L, g.area[l], ff, uf);
     return;
   }
   if (k.order == 2) load_face_state<N>(SF, m.n, F, c, U);

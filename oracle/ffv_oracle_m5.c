@@ -194,9 +194,10 @@ static void make_sol(const cfg *k, const double *U, const double *Sc, int from_f
   }
 }
 
-/* m5_bc.c:3-31: only the velocity of the ghost changes (bc_reflective.c, bc_wall.c) */
+/* m5_bc.c:3-31: only the velocity of the ghost changes (m5_bc.c:51-82 m5_bc_symmetry,
+ * bc_reflective.c, bc_wall.c) */
 static int apply_bc(int bc, const geo *g, const sol *L, sol *R) {
-  if (bc == 4 || bc == 5) {
+  if (bc == 1 || bc == 4 || bc == 5) {
     double u = L->u, v = L->v, w = L->w;
     double ul = u * g->n[0] + v * g->n[1] + w * g->n[2];
     double vl = u * g->t1[0] + v * g->t1[1] + w * g->t1[2];
@@ -208,7 +209,7 @@ static int apply_bc(int bc, const geo *g, const sol *L, sol *R) {
     return 0;
   }
   if (bc == 2 || bc == 3) return 0;  /* outlet; inlet has no model-5 state (m5_bc.c:35-48) */
-  return 9;                          /* symmetry (bc 1) needs m5_hllc.c:56-85: not restated */
+  return 9;
 }
 
 /* rotate_vectors.c:73-106: R T R^T for R with rows r0, r1, r2 (full loops) */
@@ -335,6 +336,10 @@ static void phys_flux(const cfg *k, const sol *s, int flag, int gfm, ncs *nc, do
     for (int v = 0; v < N - 1; ++v) nc->avf[v] = s->avf[v];
     for (int v = 0; v < N; ++v) nc->are[v] = s->are[v];
     for (int q = 0; q < 9; q++) nc->A[q] = gfm ? s->A[q] : -s->A[q];
+  } else if (flag == 4) { /* symmetry face: the caller gives the velocity */
+    for (int v = 0; v < N - 1; ++v) nc->avf[v] = s->avf[v];
+    for (int v = 0; v < N; ++v) nc->are[v] = s->are[v];
+    for (int q = 0; q < 9; q++) nc->A[q] = s->A[q];
   }
   for (int v = 0; v < N - 1; ++v)
     for (int d = 0; d < 3; d++) F[k->i3 + v][d] = nc->unc[d] * nc->avf[v];
@@ -737,7 +742,30 @@ static int residual(const cfg *k, const ffvo_mesh *m, const double *S, work *W) 
       double Area_f = 0.0;
       for (int q = 0; q < nneig; ++q) Area_f += m->area[4 * r + q];
       geo g = face_geo(m, c, f);
-      if (compute) {
+      if (compute && m->bc[r] == 1) {
+        /* m5_hllc.c:56-85: the HLLC flux of a symmetry face is replaced by the mean of the
+         * physical fluxes of the cell state (m5_facevalues.c, imode 0) and of its mirror
+         * image, no correction term */
+        sol L, R;
+        make_sol(k, Sc, Sc, 0, &L);
+        R = L;
+        apply_bc(1, &g, &L, &R);
+        ncs nc;
+        nc.unc[0] = 0.5 * (L.u + R.u);
+        nc.unc[1] = 0.5 * (L.v + R.v);
+        nc.unc[2] = 0.5 * (L.w + R.w);
+        double FL[MAXNEQ][3], FR[MAXNEQ][3], F[MAXNEQ][3];
+        phys_flux(k, &L, 4, 0, &nc, FL);
+        phys_flux(k, &R, 4, 0, &nc, FR);
+        for (int iv = 0; iv < neq; ++iv)
+          for (int d = 0; d < 3; d++) F[iv][d] = (0.0 + 0.5 * FL[iv][d]) + 0.5 * FR[iv][d];
+        double A = m->area[4 * r];
+        for (int iv = 0; iv < neq; ++iv)
+          ff[iv] += (A) * ((F[iv][0] * g.n[0] + F[iv][1] * g.n[1] + F[iv][2] * g.n[2]) + 0.0);
+        uf[0] = nc.unc[0];
+        uf[1] = nc.unc[1];
+        uf[2] = nc.unc[2];
+      } else if (compute) {
         sol L;
         if (k->order == 2) make_sol(k, W->SF + r * neq, Sc, 1, &L);
         else make_sol(k, Sc, Sc, 0, &L);

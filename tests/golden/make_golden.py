@@ -73,6 +73,12 @@ M5_CASES = {
                            refine="sphere 0.5 0.5 0.4 0.3 4 3", ic=WALL_IC),
     "m5_wall_rk3_order1": rc.Case(trees=(2, 2, 2), level=3, steps=3, dt=2e-8, model=5,
                                   m5=dict(WALL), rk_steps=3, order=1, ic=WALL_IC),
+    # symmetry planes (bc 1, m5_hllc.c:56-85) on three sides of a refined mesh with the
+    # moving mixture slab, the other sides transmissive or reflective
+    "m5_wall_symmetry": rc.Case(trees=(2, 2, 2), level=3, steps=4, dt=2e-7, model=5,
+                                m5=dict(WALL, mix="2 0.25 0.375 0 0.4999999 1 5e6 0 0 -50"),
+                                refine="sphere 0.5 0.5 0.4 0.3 4 3", bc=(1, 2, 4, 1, 1, 2),
+                                ic=WALL_IC),
 }
 
 

@@ -51,7 +51,7 @@ def test_m5_gpu_matches_reference_fixture(name, built_lib):
 
 
 @pytest.mark.parametrize("name,mult", [("m5_wall_amr", 3), ("m5_bubble_prelax3", 4),
-                                       ("m5_mild_prelax1", 4)])
+                                       ("m5_mild_prelax1", 4), ("m5_wall_symmetry", 3)])
 def test_m5_gpu_matches_oracle_longer(name, mult, built_lib, oracle_lib):
     """More steps than the fixture holds, against the CPU restatement (the ghost-fluid
     fixture's mixture slab stops being a valid state soon after its 4 steps: the

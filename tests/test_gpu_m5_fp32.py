@@ -66,7 +66,7 @@ def check(err, floor, keys=("rho", "p", "alpha")):
 
 CASES = [("m5_bubble_prelax3", 1), ("m5_bubble_prelax3", 3), ("m5_mild_prelax1", 3),
          ("m5_mild_prelax1", 6), ("m5_wall_rk3_order1", 3), ("m5_wall_amr", 3),
-         ("m5_wall_gfm", 2)]
+         ("m5_wall_gfm", 2), ("m5_wall_symmetry", 4)]
 
 
 @pytest.mark.parametrize("name,steps", CASES)

@@ -38,6 +38,19 @@ def test_m5_wall_fixture_exercises_ghost_fluid_fixes(oracle_lib):
     assert after[0] > before[0] and after[1] > before[1]
 
 
+def test_m5_symmetry_fixture_depends_on_the_symmetry_flux(oracle_lib):
+    """The symmetry faces' central flux (m5_hllc.c:56-85) is not the reflective HLLC flux:
+    the same run with those faces made reflective ends elsewhere."""
+    g = load_golden("m5_wall_symmetry")
+    geo = geometry_from_golden(g)
+    assert (geo["bc"] == 1).sum() > 0
+    geo["bc"] = np.where(geo["bc"] == 1, 4, geo["bc"]).astype(geo["bc"].dtype)
+    out = pyoracle.m5_advance(pyoracle.OracleMesh(geo), g["S_init"], float(g["dt"]),
+                              int(g["steps"]), m5_params(g), int(g["order"]), int(g["rk_steps"]))
+    scale = np.abs(g["S_final"]).max(axis=0) + 1e-300
+    assert (np.abs(out - g["S_final"]) / scale).max() > 1e-9
+
+
 def test_oracle_config1_sod32_bitwise(oracle_lib, built_lib):
     """32^3 Sod problem, 100 steps: oracle on the builder's geometry == reference."""
     g = load_golden("m0_config1_sod32")
