@@ -355,6 +355,8 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
       // m5_relaxationvec.c's floor -(1 - 1e-8) p_inf + 1e-8 and reset value
       k.plo_f[i] = (float)(-(1.0 - 1.0e-8) * p->pinf[i] + 1.0e-8);
       k.preset_f[i] = (float)(-(1.0 - 1.0e-8) * p->pinf[i] + 1.0);
+      // binomial series of (1 + x)^a - 1, a = -1 / gamma: ratios (a - j) / (j + 1) of its terms
+      for (int j = 1; j <= 6; j++) k.bin_f[i][j - 1] = (float)((-k.igam[i] - j) / (j + 1.0));
       k.gm1_d[i] = df_from_double(gm1);
       k.gpi_d[i] = df_from_double(k.gpi[i]);
       k.ig1_d[i] = df_from_double(k.ig1[i]);

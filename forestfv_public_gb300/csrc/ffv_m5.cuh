@@ -21,6 +21,8 @@ struct M5Consts {
   float pinf_f[FFV_MAX_MATERIALS], igam_f[FFV_MAX_MATERIALS], mu_f[FFV_MAX_MATERIALS],
       gamma_f[FFV_MAX_MATERIALS], plo_f[FFV_MAX_MATERIALS], preset_f[FFV_MAX_MATERIALS];
   float alo_f, ahi_f;
+  // (a - j) / (j + 1), j = 1..6, a = -1 / gamma: the FP32 Newton iteration's binomial series
+  float bin_f[FFV_MAX_MATERIALS][6];
   // double-float pairs for the FP32-flux form's pressure recovery: gamma - 1, gamma p_inf,
   // 1 / (gamma - 1), gamma p_inf / (gamma - 1), p_inf, the relaxation's pressure floor; and
   // AMIN / 100, 1 - AMIN / 100, 1 - 2 AMIN / 100, 1e-12, 1 - 1e-12

@@ -658,7 +658,7 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
   for (int iv = 0; iv < N; ++iv) ael[iv] = elastic_energy_f(G, Gmag, k.mu_f[iv]);
   unsigned st = 0;
   df ratio = df_make(1.0f);
-  if (k.prelax == 1) {  // closed form for two materials, in FP64
+  if (N == 2 && k.prelax == 1) {  // closed form for two materials (only), in FP64
     double a[N], t0[N], p0[N];
 #pragma unroll
     for (int iv = 0; iv < N; ++iv) {
@@ -728,7 +728,9 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
       // term keeps FP32 precision relative to its own size: summing alpha_k(p) - 1 directly
       // would resolve a 1e-6 volume fraction next to 1 - 1e-6 only to ~6e-8, which
       // p_inf = 6e8 turns into ~200 Pa.  The iterate settles within a few steps; the cap
-      // bounds the loop.
+      // bounds the loop.  Near equilibrium (|x| <= 1/32, most faces away from shocks and
+      // interfaces) e_k is the binomial series of (1 + x)^a - 1, a = -1/gamma, to x^7 in
+      // Horner form: its first omitted term is below 1e-9 of e_k for gamma >= 1.
       const float F0 = df_to_float(sum0);
       float pf = p0, F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
 #pragma unroll 1
@@ -747,10 +749,22 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
           if (live[iv]) {
             const float x = (pf - pkf[iv]) * b0[iv];
             const float opx = x > -0.5f ? 1.0f + x : fmaxf((pf + pif[iv]) * b0[iv], 1.0e-30f);
-            const float lx = x > -0.5f ? log1pf(x) : logf(opx);
-            e[iv] = expm1f(-lx * ig[iv]);
+            if (fabsf(x) <= 0.03125f) {
+              const float *cb = k.bin_f[iv];
+              float t = fmaf(cb[5] * x, 1.0f, 1.0f);
+              t = fmaf(cb[4] * x, t, 1.0f);
+              t = fmaf(cb[3] * x, t, 1.0f);
+              t = fmaf(cb[2] * x, t, 1.0f);
+              t = fmaf(cb[1] * x, t, 1.0f);
+              t = fmaf(cb[0] * x, t, 1.0f);
+              e[iv] = (-ig[iv] * x) * t;
+            } else {
+              const float lx = x > -0.5f ? log1pf(x) : logf(opx);
+              e[iv] = expm1f(-lx * ig[iv]);
+            }
             F += a0[iv] * e[iv];
-            dF -= a0[iv] * (1.0f + e[iv]) * ig[iv] * b0[iv] / opx;
+            // the derivative only steers the iteration: a fast quotient is enough
+            dF -= __fdividef(a0[iv] * (1.0f + e[iv]) * ig[iv] * b0[iv], opx);
           }
         }
         if (isnan(pf) || isnan(F) || isnan(dF)) {
@@ -849,10 +863,11 @@ __global__ void __launch_bounds__(256) m5f_shadow(int64_t n, const double *__res
   }
 }
 
-// 8 blocks of 128 threads per SM (64 registers, a few bytes of spill): the kernel is bound by
-// instruction issue, and the extra warps hide its latencies (6 % faster than 96 registers)
+// 6 blocks of 128 threads per SM (80 registers): the kernel is bound by instruction issue;
+// measured on the wall configuration, 64 registers (8 blocks) was 1.6 % slower, 96 registers
+// 6 % slower
 template <int N>
-__global__ void __launch_bounds__(128, 8) m5f_recon_face(ffv_dmesh m, ffv_geom g, M5Consts k,
+__global__ void __launch_bounds__(128, 6) m5f_recon_face(ffv_dmesh m, ffv_geom g, M5Consts k,
                                                       const float *__restrict__ Sf,
                                                       const float *__restrict__ Sflo,
                                                       float *__restrict__ SF,
@@ -876,33 +891,34 @@ __global__ void __launch_bounds__(128, 8) m5f_recon_face(ffv_dmesh m, ffv_geom g
   df cr[NCR];
   crit_load<N>(Sf, Sflo, m.n, c, cr);
   avf_limit_df<N>(k, cr);
-  value_across_f<N>(k, m, Sf, c, f, kf, sl, x);
-#pragma unroll
-  for (int i = 0; i < C::NEQ; i++) df_[i] = x[i] - sl[i];
-  value_across_f<N>(k, m, Sf, c, fo, ko, sl, x);
-  // the critical slots' differences in double-float, rounded to FP32
-  float dfc[NCR], dbc[NCR];
-  {
+  // the differences across face f (side 0) and across the opposite face (side 1); one copy
+  // of the gather code for both sides keeps the kernel small enough for the instruction cache
+  float db_[C::NEQ];
+#pragma unroll 1
+  for (int side = 0; side < 2; side++) {
+    const int fs = side ? fo : f;
+    const uint32_t ks = side ? ko : kf;
+    value_across_f<N>(k, m, Sf, c, fs, ks, sl, x);
+    // the critical slots' differences in double-float, rounded to FP32
     df xc[NCR];
-    crit_across_df<N>(k, m, Sf, Sflo, c, f, kf, cr, xc);
+    crit_across_df<N>(k, m, Sf, Sflo, c, fs, ks, cr, xc);
 #pragma unroll
-    for (int j = 0; j < NCR; j++) dfc[j] = df_to_float(df_sub(xc[j], cr[j]));
-    crit_across_df<N>(k, m, Sf, Sflo, c, fo, ko, cr, xc);
+    for (int i = 0; i < C::NEQ; i++) x[i] -= sl[i];
 #pragma unroll
-    for (int j = 0; j < NCR; j++) dbc[j] = df_to_float(df_sub(xc[j], cr[j]));
+    for (int j = 0; j < NCR; j++) x[crit_slot<N>(j)] = df_to_float(df_sub(xc[j], cr[j]));
+#pragma unroll
+    for (int i = 0; i < C::NEQ; i++) {
+      if (side == 0) df_[i] = x[i];
+      else db_[i] = x[i];
+    }
   }
-#pragma unroll
-  for (int j = 0; j < NCR; j++) df_[crit_slot<N>(j)] = dfc[j];
   const float idp = g.idcc_f[l][face_class(kf)];
   const float idm = g.idcc_f[l][face_class(ko)];
   const float cf = g.dcf_f[l][face_class(kf)];
   float corr[C::NEQ];
 #pragma unroll
   for (int i = 0; i < C::NEQ; i++) {
-    float db = x[i] - sl[i];
-#pragma unroll
-    for (int j = 0; j < NCR; j++)
-      if (i == crit_slot<N>(j)) db = dbc[j];
+    const float db = db_[i];
     float grad = 0.0f;
     if (!(kf & FFV_FK_BC) && fabsf(df_[i]) > 1e-10f && !(i >= C::i4 && i < C::i5)) {
       const float sf = df_[i] * idp, sb = -db * idm;
