@@ -28,7 +28,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from .solver import Solver, level_max, tags_smooth, would_change
+from .solver import Solver, adapt_changes, level_max, tags_smooth, would_change
 
 
 @dataclass
@@ -134,20 +134,24 @@ class AdaptiveRun:
         s.sync()
         marks = self.marks.cpu().numpy().astype(bool)
         for _ in range(self.lmax + 1):
-            raw = s.tags_raw(self.params)
-            tgt = np.where(marks, np.maximum(raw, self.pre_level), raw).astype(np.int32)
+            tgt = s.tags_raw(self.params)
+            np.maximum(tgt, self.pre_level, out=tgt, where=marks)
             tgt = tags_smooth(s.mesh, self.lmax, tgt)
-            if not would_change(s.mesh, tgt):
+            changes = adapt_changes(s.mesh, tgt)
+            if changes[0] + changes[1] == 0:
                 break
-            _, src = s.adapt(tgt, with_src=True)
-            marks = carry_marks(src, marks)
+            level = s.mesh.level
+            _, src = s.adapt(tgt, with_src=True, changes=changes)
             rounds += 1
             # every leaf at (or, for a sibling group that could not merge, above) its
             # target: no further round, whatever the criterion wants on the new state the
-            # next judge finds
-            from_leaf = src >= 0
-            if not np.any(tgt[src[from_leaf]] > s.mesh.level[from_leaf]):
+            # next judge finds.  A leaf splits exactly when its target is above its level
+            # (refineh.c:10-57), into children one level finer, and a kept leaf's target is
+            # not above its level: a new leaf from an old one is below its target only where
+            # the old leaf's target was two or more levels above it.
+            if not np.any(tgt > level + 1):
                 break
+            marks = carry_marks(src, marks)
         self.marks = None
         return rounds
 

@@ -71,7 +71,7 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
     return mx - split[c] > 1 ? mx - 1 : split[c];
   };
   // A sweep updates split in place in leaf order, each leaf seeing its predecessors' new
-  // values.  It runs as a worklist with the same result: the leaves are first evaluated on
+  // values.  The 2:1 rule's sweep runs as a worklist with the same result: the leaves are first evaluated on
   // the sweep's input in parallel, and those whose value would change are visited in leaf
   // order; when a visited leaf changes, the later leaves that read its value (its sibling
   // group for the coarsening rule, its face neighbours for the 2:1 rule) join the worklist.
@@ -150,10 +150,87 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
     }
     return true;
   };
+  // The coarsening rule reads only the leaf's own sibling group, and a group's eight leaves
+  // are consecutive in leaf order: its in-order sweep is the groups' own in-order sweeps,
+  // independent of one another.  It runs in parallel over chunks that start and end on group
+  // boundaries, each group in order.  A leaf's rule only reads its group when some leaf of
+  // the eight is below its level; otherwise the leaves are swept one by one.  A group that
+  // changed is evaluated again at the next pass (its earlier leaves read the later ones' old
+  // values), one that did not is a fixed point until an input changes.
+  auto align = [&](int64_t x) -> int64_t {
+    if (x <= 0 || x >= n) return x;
+    const int64_t g = ffv_sibling_group(m, x);
+    return g >= 0 ? g : x;
+  };
+  std::vector<int32_t> changed_in(n, -1);  // the pass in which the coarsening rule changed it
+  auto sweep1 = [&](int32_t pass) -> bool {
+    std::vector<uint8_t> any(nth, 0);
+    parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
+      a = align(a);
+      b = align(b);
+      auto visit = [&](int64_t c) -> bool {
+        const int32_t v = rule1(c);
+        if (v == split[c]) return false;
+        split[c] = v;
+        changed_in[c] = pass;
+        any[t] = 1;
+        return true;
+      };
+      for (int64_t c = a; c < b;) {
+        const int32_t *x = m->cell_ijk + 3 * c;
+        bool below = false;
+        if ((x[0] & 1) == 0 && (x[1] & 1) == 0 && (x[2] & 1) == 0 && c + 8 <= b)
+          for (int64_t q = c; q < c + 8 && !below; q++) below = split[q] < level(q);
+        if (below && group_of(c) == c) {
+          bool dirty = false;
+          for (int64_t q = c; q < c + 8; q++) dirty = dirty || dirty1[q];
+          if (dirty) {
+            bool ch = false;
+            for (int64_t q = c; q < c + 8; q++) {
+              dirty1[q] = 0;
+              ch = visit(q) || ch;
+            }
+            if (ch)
+              for (int64_t q = c; q < c + 8; q++) dirty1[q] = 1;
+          }
+          c += 8;
+        } else {
+          if (dirty1[c]) {
+            dirty1[c] = 0;
+            visit(c);
+          }
+          c++;
+        }
+      }
+    });
+    bool changed = false;
+    for (int t = 0; t < nth; t++) changed = changed || any[t];
+    if (!changed) return false;
+    // the 2:1 rule's readers of a changed leaf: itself and its face neighbours (the face
+    // relation is symmetric), gathered by each reader
+    parallel_chunks(n, nth, [&](int, int64_t a, int64_t b) {
+      for (int64_t c = a; c < b; c++) {
+        bool hit = changed_in[c] == pass;
+        const uint32_t info = m->info[c];
+        for (int f = 0; f < 6 && !hit; f++) {
+          const uint32_t kind = ffv_face_kind(info, f);
+          if (kind & FFV_FK_BC) continue;
+          const int32_t s = m->nbr[6 * c + f];
+          if (kind == FFV_FK_FINER) {
+            for (int q = 0; q < 4; q++) hit = hit || changed_in[m->sub[4 * (int64_t)s + q]] == pass;
+          } else {
+            hit = changed_in[s] == pass;
+          }
+        }
+        if (hit) dirty2[c] = 1;
+      }
+    });
+    return true;
+  };
   // A pass is a function of `split` alone: once one changes nothing, every later pass
   // would see the same input and change nothing either, so the passes end there.
   for (int32_t pass = 0; pass < level_max + 1; pass++) {
-    const bool c1 = sweep(rule1, true, dirty1, dirty2);
+    const bool c1 = sweep1(pass);
     const bool c2 = sweep(rule2, false, dirty2, dirty1);
     if (!c1 && !c2) break;
   }

@@ -160,17 +160,18 @@ class Solver:
                                               ctypes.byref(out)), "ffv_tags_missed")
         return int(out.value)
 
-    def adapt(self, split, with_src: bool = False):
+    def adapt(self, split, with_src: bool = False, changes: tuple[int, int] | None = None):
         """One refineh pass (ffv_adapt) with target levels `split`; the solver continues on
         the returned mesh with the carried-over state.  with_src also returns every new
         leaf's source (ffv_adapt_map: the old leaf it copies, or -1 - j for a parent merged
-        from old leaves j..j+7)."""
+        from old leaves j..j+7); `changes`, when the caller has them, are adapt_changes of
+        `split` (they size the source array)."""
         split = np.ascontiguousarray(split, dtype=np.int32)
         assert split.shape == (self.mesh.n,)
         h = ctypes.c_void_p()
         src = None
         if with_src:
-            ns, nm = adapt_changes(self.mesh, split)
+            ns, nm = changes if changes is not None else adapt_changes(self.mesh, split)
             src = np.empty(self.mesh.n + 7 * (ns - nm), np.int64)
         _lib.check(_lib.lib().ffv_adapt_map(self._h, self.mesh.handle, split.ctypes.data,
                                             ctypes.byref(h),
