@@ -127,12 +127,16 @@ extern "C" int ffv_adapt(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split, 
   return ffv_adapt_map(ctx, m, split, out, nullptr);
 }
 
-// the leaves of a mesh in its cell order (the inverse of ffv_mesh_build's input)
+// the leaves of a mesh in its cell order (the inverse of ffv_mesh_build's input); any of the
+// three outputs may be null
 extern "C" int ffv_mesh_leaves(const ffv_mesh *m, int32_t *tree_ijk, int32_t *level,
                                int32_t *cell_ijk) {
-  if (!m || !tree_ijk || !level || !cell_ijk) return FFV_ERR_ARG;
-  memcpy(tree_ijk, m->tree_ijk, sizeof(int32_t) * 3 * m->n);
-  memcpy(cell_ijk, m->cell_ijk, sizeof(int32_t) * 3 * m->n);
-  for (int64_t c = 0; c < m->n; c++) level[c] = ffv_info_level(m->info[c]);
+  if (!m || (!tree_ijk && !level && !cell_ijk)) return FFV_ERR_ARG;
+  if (tree_ijk) memcpy(tree_ijk, m->tree_ijk, sizeof(int32_t) * 3 * m->n);
+  if (cell_ijk) memcpy(cell_ijk, m->cell_ijk, sizeof(int32_t) * 3 * m->n);
+  if (level)
+    parallel_chunks(m->n, host_threads(), [&](int, int64_t a, int64_t b) {
+      for (int64_t c = a; c < b; c++) level[c] = ffv_info_level(m->info[c]);
+    });
   return FFV_OK;
 }

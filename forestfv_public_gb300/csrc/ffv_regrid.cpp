@@ -31,7 +31,8 @@ constexpr int kDepth = FFV_MAX_LEVEL - 1;  // Morton digits below the tree at th
 struct Leaves {
   int32_t *tij = nullptr, *cij = nullptr;  // new leaves in leaf order (the new mesh's arrays)
   std::vector<int32_t> lev;
-  std::vector<int64_t> src;      // old leaf copied or split (>= 0), -1 - j merged from j..j+7
+  int64_t *src = nullptr;        // old leaf copied or split (>= 0), -1 - j merged from j..j+7
+  std::vector<int64_t> own_src;  // src's storage when the caller does not want it
   std::vector<int32_t> old2new;  // kept old leaves' new index, else -1
   std::vector<uint8_t> what;     // per old leaf: 0 absorbed, 1 kept, 2 merged parent, 8 split
   std::vector<int64_t> tsum;     // new leaves before each chunk of old leaves
@@ -74,7 +75,6 @@ void fill_leaves(const ffv_mesh *m, int nth, Leaves &L) {
   const int64_t n = m->n, nn = L.nn;
   const std::vector<int64_t> &tsum = L.tsum;
   L.lev.resize(nn);
-  L.src.resize(nn);
   L.old2new.resize(n);
   parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
     int64_t o = tsum[t];
@@ -157,6 +157,12 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
   }
   L.tij = nm->tree_ijk;
   L.cij = nm->cell_ijk;
+  if (src) {
+    L.src = src;
+  } else {
+    L.own_src.resize(nn);
+    L.src = L.own_src.data();
+  }
   fill_leaves(m, nth, L);
   const int32_t *NT = m->desc.ntrees;
   const std::vector<uint64_t> rank = tree_ranks(NT);
@@ -174,26 +180,25 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
                       (uint32_t)((g[1] - (t1 << (l - 1))) << sh),
                       (uint32_t)((g[2] - (t2 << (l - 1))) << sh));
   };
-  std::vector<uint64_t> key(nn);
-  std::vector<char> unsorted(nth, 0);
-  parallel_chunks(nn, nth, [&](int, int64_t a, int64_t b) {
-    for (int64_t j = a; j < b; j++) {
-      const int l = L.lev[j];
-      const int64_t g[3] = {((int64_t)L.tij[3 * j] << (l - 1)) + L.cij[3 * j],
-                            ((int64_t)L.tij[3 * j + 1] << (l - 1)) + L.cij[3 * j + 1],
-                            ((int64_t)L.tij[3 * j + 2] << (l - 1)) + L.cij[3 * j + 2]};
-      key[j] = point_key(l, g);
-    }
-  });
-  parallel_chunks(nn > 0 ? nn - 1 : 0, nth, [&](int t, int64_t a, int64_t b) {
-    for (int64_t j = a; j < b && !unsorted[t]; j++) unsorted[t] = !(key[j] < key[j + 1]);
-  });
-  if (std::any_of(unsorted.begin(), unsorted.end(), [](char x) { return x != 0; })) {
-    ffv_mesh_free(nm);
-    return FFV_ERR_TABLE;
-  }
+  auto key_of = [&](int64_t j) {
+    const int l = L.lev[j];
+    const int64_t g[3] = {((int64_t)L.tij[3 * j] << (l - 1)) + L.cij[3 * j],
+                          ((int64_t)L.tij[3 * j + 1] << (l - 1)) + L.cij[3 * j + 1],
+                          ((int64_t)L.tij[3 * j + 2] << (l - 1)) + L.cij[3 * j + 2]};
+    return point_key(l, g);
+  };
+  // the new leaves' keys ascend in leaf order: the old leaves' did (the builder sorts them),
+  // and a split's children or a merge's parent take the key range of what they replace.  The
+  // keys are formed during the search, for the few leaves that search: the last leaf whose
+  // key is not above pk
   auto find = [&](uint64_t pk) {
-    return (int64_t)(std::upper_bound(key.begin(), key.end(), pk) - key.begin()) - 1;
+    int64_t lo = 0, hi = nn;  // the answer + 1 lies in [lo, hi]
+    while (lo < hi) {
+      const int64_t mid = lo + (hi - lo) / 2;
+      if (key_of(mid) <= pk) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo - 1;
   };
   // old leaves whose rows can be copied: kept, and no face neighbour splits or merges
   const int64_t n = m->n;
@@ -305,32 +310,27 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
     ffv_mesh_free(nm);
     return rc;
   }
-  // subface groups numbered in cell order: each chunk's groups shifted by the groups before it
-  std::vector<int32_t> sub;
-  size_t total = 0;
-  for (auto &v : csub) total += v.size();
-  sub.reserve(total);
-  for (int t = 0; t < nth; t++) {
-    const int32_t off = (int32_t)(sub.size() / 4);
-    if (off) {
-      const int64_t c0 = std::min(nn, (int64_t)t * chunk), c1 = std::min(nn, (int64_t)(t + 1) * chunk);
-      for (int64_t c = c0; c < c1; c++)
-        for (int f = 0; f < 6; f++)
-          if (ffv_face_kind(nm->info[c], f) == FFV_FK_FINER) nm->nbr[6 * c + f] += off;
-    }
-    sub.insert(sub.end(), csub[t].begin(), csub[t].end());
-  }
-  nm->nsub = (int32_t)(sub.size() / 4);
-  nm->sub = (int32_t *)malloc(sizeof(int32_t) * (sub.size() ? sub.size() : 4));
+  // subface groups numbered in cell order: each chunk's groups shifted by the groups before
+  // it (the chunks are parallel_chunks' over nn, as above)
+  std::vector<size_t> off(nth + 1, 0);
+  for (int t = 0; t < nth; t++) off[t + 1] = off[t] + csub[t].size();
+  nm->nsub = (int32_t)(off[nth] / 4);
+  nm->sub = (int32_t *)malloc(sizeof(int32_t) * (off[nth] ? off[nth] : 4));
   if (!nm->sub) {
     ffv_mesh_free(nm);
     return FFV_ERR_NOMEM;
   }
-  if (!sub.empty()) memcpy(nm->sub, sub.data(), sizeof(int32_t) * sub.size());
+  parallel_chunks(nn, nth, [&](int t, int64_t a, int64_t b) {
+    const int32_t shift = (int32_t)(off[t] / 4);
+    if (shift)
+      for (int64_t c = a; c < b; c++)
+        for (int f = 0; f < 6; f++)
+          if (ffv_face_kind(nm->info[c], f) == FFV_FK_FINER) nm->nbr[6 * c + f] += shift;
+    if (!csub[t].empty()) memcpy(nm->sub + off[t], csub[t].data(), sizeof(int32_t) * csub[t].size());
+  });
   nm->min_level = *std::min_element(tmin.begin(), tmin.end());
   nm->max_level = *std::max_element(tmax.begin(), tmax.end());
   if (nn == 0) nm->min_level = nm->max_level = 0;
-  if (src) memcpy(src, L.src.data(), sizeof(int64_t) * nn);
   *out = nm;
   return FFV_OK;
 }

@@ -86,16 +86,15 @@ class Mesh:
         tij = np.ascontiguousarray(leaves.tree_ijk, dtype=np.int32)
         lev = np.ascontiguousarray(leaves.level, dtype=np.int32)
         cij = np.ascontiguousarray(leaves.cell_ijk, dtype=np.int32)
-        self.order = np.zeros(leaves.n, dtype=np.int64)
+        self._order = np.zeros(leaves.n, dtype=np.int64)
         h = ctypes.c_void_p()
         _lib.check(L.ffv_mesh_build(ctypes.byref(d), leaves.n, tij.ctypes.data, lev.ctypes.data,
-                                    cij.ctypes.data, ctypes.byref(h), self.order.ctypes.data),
+                                    cij.ctypes.data, ctypes.byref(h), self._order.ctypes.data),
                    "ffv_mesh_build")
         self._h = h
         self.n = int(L.ffv_mesh_ncells(h))
-        self.level = lev[self.order]
-        self.tree_ijk = tij[self.order]
-        self.cell_ijk = cij[self.order]
+        self.level = lev[self._order]
+        self._coords = (tij[self._order], cij[self._order])
 
     @classmethod
     def from_handle(cls, h, ntrees, bc, tree_edge) -> "Mesh":
@@ -105,13 +104,36 @@ class Mesh:
         m.ntrees, m.bc, m.tree_edge = tuple(ntrees), tuple(bc), float(tree_edge)
         m._h = h
         m.n = int(L.ffv_mesh_ncells(h))
-        m.tree_ijk = np.empty((m.n, 3), np.int32)
-        m.cell_ijk = np.empty((m.n, 3), np.int32)
         m.level = np.empty(m.n, np.int32)
-        _lib.check(L.ffv_mesh_leaves(h, m.tree_ijk.ctypes.data, m.level.ctypes.data,
-                                     m.cell_ijk.ctypes.data), "ffv_mesh_leaves")
-        m.order = np.arange(m.n, dtype=np.int64)
+        _lib.check(L.ffv_mesh_leaves(h, None, m.level.ctypes.data, None), "ffv_mesh_leaves")
+        m._coords = None  # the leaves' coordinates, copied on first use
+        m._order = None
         return m
+
+    def _leaf_coords(self):
+        if self._coords is None:
+            t = np.empty((self.n, 3), np.int32)
+            c = np.empty((self.n, 3), np.int32)
+            _lib.check(_lib.lib().ffv_mesh_leaves(self._h, t.ctypes.data, None, c.ctypes.data),
+                       "ffv_mesh_leaves")
+            self._coords = (t, c)
+        return self._coords
+
+    @property
+    def tree_ijk(self) -> np.ndarray:
+        return self._leaf_coords()[0]
+
+    @property
+    def cell_ijk(self) -> np.ndarray:
+        return self._leaf_coords()[1]
+
+    @property
+    def order(self) -> np.ndarray:
+        """Leaf-list position of each input leaf (the identity for tables the library
+        built itself)."""
+        if self._order is None:
+            self._order = np.arange(self.n, dtype=np.int64)
+        return self._order
 
     @property
     def handle(self):

@@ -214,7 +214,8 @@ int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh **out, int6
 /* What one refineh pass with targets split[n] would do (host, no GPU): the number of
  * leaves that split and of sibling groups that merge.  Both 0: the pass changes nothing. */
 int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_t *nsplit, int64_t *nmerge);
-/* The leaves of a mesh in its cell order (tree_ijk[3n], level[n], cell_ijk[3n]). */
+/* The leaves of a mesh in its cell order (tree_ijk[3n], level[n], cell_ijk[3n]); an output
+ * may be null (not all three). */
 int ffv_mesh_leaves(const ffv_mesh *m, int32_t *tree_ijk, int32_t *level, int32_t *cell_ijk);
 
 /* Global conservation sums in FP64: sums[v] = sum over leaves of |V| S[v] for every conserved
