@@ -18,7 +18,7 @@ One benchmark step is one time step (all RK stages) over the whole mesh; one cel
 is one cell advanced one time step.
 
   value      the metric's form: the FP32-flux form with learned AMR over `steps` steps of
-             the time loop (network every step, the plain criterion as judge every 8 steps,
+             the time loop (network every 4 steps, the plain criterion as judge every 8 steps,
              regrids when it finds cells to refine), CUDA events on the solver's stream
              around the loop (judges and regrids included); state resident in HBM
   plain_fp64_amr  the comparator: plain FP64 with the reference's AMR (meshadaptation
@@ -158,11 +158,14 @@ def wl_config3(small: bool = False, medium: bool = False):
            "parallelism": "single GPU",
            "l2": f"state {state_mb:.0f} MB > L2 (129 MB): no flush needed"}
     cfg["amr"] = {"tags": list(wall_tags(lmax)), "every": AMR_EVERY, "horizon": AMR_HORIZON,
-                  "threshold": AMR_THRESHOLD}
+                  "threshold": AMR_THRESHOLD, "infer_every": AMR_INFER_EVERY}
     return mesh, S0, dt, cfg, _wall_solver_kwargs(p), m5_alg_bytes(neq, 3), False
 
 
 AMR_EVERY, AMR_HORIZON, AMR_THRESHOLD = 8, 16, 0.3
+# the network runs every fourth step: a mark predicts a refinement within AMR_HORIZON steps,
+# and the marks accumulate until the next regrid
+AMR_INFER_EVERY = 4
 WALL_LRS = 16
 
 
@@ -518,8 +521,7 @@ def amr_launches(solver, st, judge_launches: int) -> int:
     """Kernel launches of an AdaptiveRun's steps, judges and inferences (regrids not
     counted): launches per step x steps, judge_launches per judge, 3 per inference
     (fields, gather, forward)."""
-    infer = st.steps if st.t_infer > 0 else 0
-    return solver.launches_per_step() * st.steps + judge_launches * st.judged + 3 * infer
+    return solver.launches_per_step() * st.steps + judge_launches * st.judged + 3 * st.inferences
 
 
 def run_ours(args) -> None:
@@ -665,7 +667,7 @@ def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, ke
     """The metric's two forms over the time loop with mesh adaptation, both from the
     criterion-adapted mesh and state: plain FP64 with plain AMR (the reference's loop,
     meshadaptation every `every` steps) and the FP32-flux form with learned AMR (network
-    every step, the criterion as judge every `every` steps, regrids only when it finds
+    every `infer_every` steps, the criterion as judge every `every` steps, regrids only when it finds
     cells to refine or after three skips).  Returns the keys of the headline line."""
     import torch
 
@@ -691,7 +693,8 @@ def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, ke
     sec_p, cu_p, _, _ = timed_amr_loop(sp, plain, dt, args.steps, args.warmup, st_p)
     # FP32 flux + learned AMR
     sl = fresh(1)
-    learned = AdaptiveRun(sl, tags, every=every, indicator=ind, threshold=thr)
+    learned = AdaptiveRun(sl, tags, every=every, indicator=ind, threshold=thr,
+                          infer_every=amr_cfg.get("infer_every", 1))
     st_l = torch.cuda.ExternalStream(sl.stream_handle(), device=dev)
     sec_l, cu_l, _, _ = timed_amr_loop(sl, learned, dt, args.steps, args.warmup, st_l)
     mu = kw.get("mu")
@@ -704,7 +707,8 @@ def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, ke
     # the learned form end to end: state uploaded from and downloaded to pinned host memory
     # around every step of the same loop
     se = fresh(1)
-    e2e_run = AdaptiveRun(se, tags, every=every, indicator=ind, threshold=thr)
+    e2e_run = AdaptiveRun(se, tags, every=every, indicator=ind, threshold=thr,
+                            infer_every=amr_cfg.get("infer_every", 1))
     st_e = torch.cuda.ExternalStream(se.stream_handle(), device=dev)
     sec_e, cu_e, h2d, d2h = timed_amr_loop(se, e2e_run, dt, args.steps, args.warmup, st_e,
                                            host=True)
@@ -723,6 +727,7 @@ def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, ke
                            "amr": plain.stats.as_dict()},
         "learned_amr": {"amr": learned.stats.as_dict(), "indicator_training": train,
                         "every": every, "horizon": amr_cfg["horizon"], "threshold": thr,
+                        "infer_every": amr_cfg.get("infer_every", 1),
                         "error_vs_plain_fp64_amr": err,
                         "speedup_vs_plain_fp64_amr": value / plain_value},
     }

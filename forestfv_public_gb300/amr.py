@@ -45,6 +45,7 @@ class AMRStats:
     t_regrid: float = 0.0
     t_judge: float = 0.0
     t_infer: float = 0.0
+    inferences: int = 0
 
     @property
     def seconds(self) -> float:
@@ -57,7 +58,7 @@ class AMRStats:
                 "cells_min": int(min(self.cells)) if self.cells else 0,
                 "cells_max": int(max(self.cells)) if self.cells else 0,
                 "seconds": self.seconds, "step_s": self.t_step, "regrid_s": self.t_regrid,
-                "judge_s": self.t_judge, "infer_s": self.t_infer,
+                "judge_s": self.t_judge, "infer_s": self.t_infer, "inferences": self.inferences,
                 "cell_updates_per_s": self.cell_updates / max(self.seconds, 1e-30)}
 
 
@@ -184,6 +185,7 @@ class AdaptiveRun:
             if self.indicator is not None and k % self.infer_every == 0:
                 t0 = time.perf_counter()
                 self._mark(accumulate=True)
+                st.inferences += 1
                 st.t_infer += time.perf_counter() - t0
             t0 = time.perf_counter()
             s.step(dt, 1)

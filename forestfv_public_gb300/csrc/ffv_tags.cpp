@@ -162,7 +162,9 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
     const int64_t g = ffv_sibling_group(m, x);
     return g >= 0 ? g : x;
   };
-  std::vector<int32_t> changed_in(n, -1);  // the pass in which the coarsening rule changed it
+  // 1 + the pass in which the coarsening rule last changed the leaf, modulo 256 (a stale
+  // equal value after 256 passes would only make a leaf dirty that need not be)
+  std::vector<uint8_t> changed_in(n, 0);
   auto sweep1 = [&](int32_t pass) -> bool {
     std::vector<uint8_t> any(nth, 0);
     parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
@@ -172,7 +174,7 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
         const int32_t v = rule1(c);
         if (v == split[c]) return false;
         split[c] = v;
-        changed_in[c] = pass;
+        changed_in[c] = (uint8_t)(pass + 1);
         any[t] = 1;
         return true;
       };
@@ -210,16 +212,17 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
     // relation is symmetric), gathered by each reader
     parallel_chunks(n, nth, [&](int, int64_t a, int64_t b) {
       for (int64_t c = a; c < b; c++) {
-        bool hit = changed_in[c] == pass;
+        const uint8_t mark = (uint8_t)(pass + 1);
+        bool hit = changed_in[c] == mark;
         const uint32_t info = m->info[c];
         for (int f = 0; f < 6 && !hit; f++) {
           const uint32_t kind = ffv_face_kind(info, f);
           if (kind & FFV_FK_BC) continue;
           const int32_t s = m->nbr[6 * c + f];
           if (kind == FFV_FK_FINER) {
-            for (int q = 0; q < 4; q++) hit = hit || changed_in[m->sub[4 * (int64_t)s + q]] == pass;
+            for (int q = 0; q < 4; q++) hit = hit || changed_in[m->sub[4 * (int64_t)s + q]] == mark;
           } else {
-            hit = changed_in[s] == pass;
+            hit = changed_in[s] == mark;
           }
         }
         if (hit) dirty2[c] = 1;
