@@ -251,7 +251,9 @@ extern "C" int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_
     for (int64_t c = a; c < b; c++) {
       const int32_t l = (int32_t)ffv_info_level(m->info[c]);
       if (split[c] > l) ns[t]++;
-      if (l > 1 && ffv_sibling_group(m, c) == c) {
+      // a group merges only if its first leaf (like all eight) wants a coarser level: the
+      // group is looked up only then
+      if (l > 1 && split[c] < l && ffv_sibling_group(m, c) == c) {
         bool all = true;
         for (int q = 0; q < 8 && all; q++) all = split[c + q] < l;
         nm[t] += all ? 1 : 0;
