@@ -85,10 +85,14 @@ def _smooth_sequential(m, lmax, split):
     return split
 
 
-@pytest.mark.parametrize("seed", [3, 4, 5])
-def test_smoothing_equals_sequential_sweeps(seed, built_lib):
-    """The worklist smoothing (parallel evaluation of dirty leaves, in-place visits in leaf
-    order) against the plain sequential sweeps, on random targets of an AMR forest."""
+@pytest.mark.parametrize("seed,mode", [(3, "noise"), (4, "noise"), (5, "noise"),
+                                       (6, "groups"), (7, "groups"), (8, "coarsen")])
+def test_smoothing_equals_sequential_sweeps(seed, mode, built_lib):
+    """The smoothing as built (the coarsening rule's sweep in parallel over sibling groups,
+    the 2:1 rule's as a worklist after a parallel evaluation of dirty leaves) against the
+    plain sequential sweeps, on random targets of an AMR forest: independent noise per
+    leaf, one random offset per group of eight consecutive leaves (whole groups that want
+    to coarsen, next to groups that do not), and targets mostly below the level."""
     from forestfv_public_gb300 import Mesh
     from forestfv_public_gb300.solver import tags_smooth
     from forestfv_public_gb300.workloads import refine_to_target
@@ -97,5 +101,12 @@ def test_smoothing_equals_sequential_sweeps(seed, built_lib):
         c[:, 0] < 0.25, 4, np.where(c[:, 0] < 0.5, 3, 2)))
     m = Mesh((2, 2, 2), leaves)
     lmax = 6
-    split = np.clip(m.level + rng.integers(-2, 3, m.n), 1, lmax).astype(np.int32)
+    if mode == "noise":
+        d = rng.integers(-2, 3, m.n)
+    elif mode == "groups":
+        d = np.repeat(rng.integers(-2, 2, (m.n + 7) // 8), 8)[:m.n]
+        d = d + (rng.random(m.n) < 0.05) * rng.integers(-1, 2, m.n)
+    else:
+        d = -rng.integers(0, 3, m.n) + (rng.random(m.n) < 0.02)
+    split = np.clip(m.level + d, 1, lmax).astype(np.int32)
     assert np.array_equal(tags_smooth(m, lmax, split), _smooth_sequential(m, lmax, split))
