@@ -165,17 +165,18 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   // 1 + the pass in which the coarsening rule last changed the leaf, modulo 256 (a stale
   // equal value after 256 passes would only make a leaf dirty that need not be)
   std::vector<uint8_t> changed_in(n, 0);
+  std::vector<std::vector<int64_t>> chg(nth);  // the leaves each thread's sweep changed
   auto sweep1 = [&](int32_t pass) -> bool {
-    std::vector<uint8_t> any(nth, 0);
     parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
       a = align(a);
       b = align(b);
+      chg[t].clear();
       auto visit = [&](int64_t c) -> bool {
         const int32_t v = rule1(c);
         if (v == split[c]) return false;
         split[c] = v;
         changed_in[c] = (uint8_t)(pass + 1);
-        any[t] = 1;
+        chg[t].push_back(c);
         return true;
       };
       for (int64_t c = a; c < b;) {
@@ -205,11 +206,17 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
         }
       }
     });
-    bool changed = false;
-    for (int t = 0; t < nth; t++) changed = changed || any[t];
-    if (!changed) return false;
-    // the 2:1 rule's readers of a changed leaf: itself and its face neighbours (the face
-    // relation is symmetric), gathered by each reader
+    size_t nchg = 0;
+    for (int t = 0; t < nth; t++) nchg += chg[t].size();
+    if (nchg == 0) return false;
+    // the 2:1 rule's readers of a changed leaf: itself and its face neighbours -- marked
+    // from the lists when they are short, else gathered by each reader over all leaves (the
+    // face relation is symmetric)
+    if ((int64_t)nchg * 16 < n) {
+      for (int t = 0; t < nth; t++)
+        for (int64_t c : chg[t]) mark_deps(c, false, false, [&](int64_t d) { dirty2[d] = 1; });
+      return true;
+    }
     parallel_chunks(n, nth, [&](int, int64_t a, int64_t b) {
       for (int64_t c = a; c < b; c++) {
         const uint8_t mark = (uint8_t)(pass + 1);
