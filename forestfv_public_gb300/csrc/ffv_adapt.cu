@@ -69,19 +69,18 @@ extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *spl
   // the new leaves and their tables (host; rows of leaves the pass leaves alone are the old
   // ones renumbered), then the state carried over on the device
   ffv_mesh *nm = nullptr;
-  std::vector<int64_t> cmap;
-  {
-    int64_t ns = 0, nmg = 0;
-    rc = ffv_adapt_changes(m, split, &ns, &nmg);
-    if (rc != FFV_OK) return rc;
-    cmap.resize(m->n + 7 * (ns - nmg));
+  std::vector<int64_t> own_map;
+  int64_t *cmap = src;  // every new leaf's source: the caller's array, else one of our own
+  int64_t nsplit = 0, nmerged = 0;  // leaves that split, merged parents
+  rc = ffv_adapt_changes(m, split, &nsplit, &nmerged);
+  if (rc != FFV_OK) return rc;
+  if (!cmap) {
+    own_map.resize(m->n + 7 * (nsplit - nmerged));
+    cmap = own_map.data();
   }
-  rc = ffv_mesh_adapt(m, split, &nm, cmap.data());
+  rc = ffv_mesh_adapt(m, split, &nm, cmap);
   if (rc != FFV_OK) return rc;
   const int64_t n_new = nm->n;
-  int64_t nmerged = 0;
-  for (int64_t j = 0; j < n_new; j++) nmerged += cmap[j] < 0 ? 1 : 0;
-  if (src) memcpy(src, cmap.data(), sizeof(int64_t) * n_new);
   // carry the state over on the device, then swap the tables
   cudaError_t e = cudaSetDevice(device);
   int64_t *d_map = nullptr;
@@ -89,7 +88,7 @@ extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *spl
   if (e == cudaSuccess) e = cudaMalloc(&d_map, sizeof(int64_t) * n_new);
   if (e == cudaSuccess) e = cudaMalloc(&d_T, sizeof(double) * neq * n_new);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_map, cmap.data(), sizeof(int64_t) * n_new, cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(d_map, cmap, sizeof(int64_t) * n_new, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
     adapt_remap<<<152 * 4, 256, 0, st>>>(n_new, n, neq, d_map, d_S, d_T);
     e = cudaGetLastError();
