@@ -76,7 +76,7 @@ def build(verbose: bool = False) -> str:
 
 
 def build_oracle() -> str:
-    """CPU restatement used by the tests as the checker (oracle/_build/libffv_oracle.so)."""
+    """CPU restatement the tests check the CUDA path against (oracle/_build/libffv_oracle.so)."""
     odir = os.path.join(ROOT, "oracle")
     out = os.path.join(odir, "_build")
     os.makedirs(out, exist_ok=True)

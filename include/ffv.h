@@ -43,7 +43,7 @@ extern "C" {
 #define FFV_ERR_NAN 5          /* non-finite residual or state found on the device       */
 #define FFV_ERR_NEG_DENSITY 6  /* non-positive density found on the device               */
 #define FFV_ERR_TIMEOUT 7      /* a bounded device wait ran out                          */
-#define FFV_ERR_UNSUPPORTED 8  /* option outside what this build implements              */
+#define FFV_ERR_UNSUPPORTED 8  /* option outside what this library implements            */
 #define FFV_ERR_NOMEM 9        /* host or device allocation failed                       */
 #define FFV_ERR_STATE 10       /* call out of order (e.g. step before mesh/state upload) */
 #define FFV_ERR_TOO_LARGE 11   /* mesh larger than the fixed scratch of ffv_step_noalloc */

@@ -1,4 +1,4 @@
-"""CPU restatement of the learned refinement indicator (test infrastructure: the checker of
+"""CPU restatement of the learned refinement indicator (test infrastructure: the oracle for
 the CUDA kernels in forestfv_public_gb300/csrc/ffv_mlp.cu, never the thing measured).
 
 The indicator has no counterpart in the reference; this restates its equations in float64

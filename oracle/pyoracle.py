@@ -1,6 +1,6 @@
 """ctypes binding of the CPU restatement (oracle/_build/libffv_oracle.so).
 
-TEST INFRASTRUCTURE: the checker for the CUDA path, used only by tests/,
+TEST INFRASTRUCTURE: the oracle for the CUDA path, used only by tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline leg.
 """
 from __future__ import annotations
