@@ -200,28 +200,23 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
     }
     return lo - 1;
   };
-  // old leaves whose rows can be copied: kept, and no face neighbour splits or merges
-  const int64_t n = m->n;
-  std::vector<uint8_t> copy(n, 0);
-  parallel_chunks(n, nth, [&](int, int64_t a, int64_t b) {
-    for (int64_t c = a; c < b; c++) {
-      if (L.what[c] != 1) continue;
-      bool ok = true;
-      const uint32_t info = m->info[c];
-      for (int f = 0; f < 6 && ok; f++) {
-        const uint32_t kind = ffv_face_kind(info, f);
-        if (kind & FFV_FK_BC) continue;
-        const int32_t s = m->nbr[6 * c + f];
-        if (kind == FFV_FK_FINER) {
-          for (int q = 0; q < 4; q++) ok = ok && L.what[m->sub[4 * (int64_t)s + q]] == 1;
-        } else {
-          ok = L.what[s] == 1;
-        }
+  // an old leaf whose rows can be copied: kept, and no face neighbour splits or merges
+  auto copyable = [&](int64_t c) {
+    if (L.what[c] != 1) return false;
+    const uint32_t info = m->info[c];
+    for (int f = 0; f < 6; f++) {
+      const uint32_t kind = ffv_face_kind(info, f);
+      if (kind & FFV_FK_BC) continue;
+      const int32_t s = m->nbr[6 * c + f];
+      if (kind == FFV_FK_FINER) {
+        for (int q = 0; q < 4; q++)
+          if (L.what[m->sub[4 * (int64_t)s + q]] != 1) return false;
+      } else if (L.what[s] != 1) {
+        return false;
       }
-      copy[c] = ok ? 1 : 0;
     }
-  });
-
+    return true;
+  };
 
   const int64_t chunk = (nn + nth - 1) / (nth ? nth : 1);
   std::vector<std::vector<int32_t>> csub(nth);
@@ -234,7 +229,7 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
       tmin[t] = std::min(tmin[t], l);
       tmax[t] = std::max(tmax[t], l);
       const int64_t s = L.src[j];
-      if (s >= 0 && L.what[s] == 1 && copy[s]) {  // the old rows, renumbered
+      if (s >= 0 && copyable(s)) {  // the old rows, renumbered
         const uint32_t info = m->info[s];
         for (int f = 0; f < 6; f++) {
           const uint32_t kind = ffv_face_kind(info, f);
