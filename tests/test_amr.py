@@ -85,3 +85,37 @@ def test_mesh_adapt_equals_full_build(seed, built_lib):
         assert np.all((new.level[keep] == lev_old[src[keep]]) | (new.level[keep] == lev_old[src[keep]] + 1))
         assert np.all(new.level[~keep] == lev_old[-1 - src[~keep]] - 1)
         m = new
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_round_end_check_from_old_levels(seed, built_lib):
+    """The learned regrid ends its rounds when no new leaf from an old one is below the old
+    leaf's target.  It decides that from the old levels alone (a leaf splits exactly when its
+    target is above its level, one level at a time): any(target > level + 1).  Both forms
+    agree on smoothed random passes and on passes that split isolated leaves of a uniform
+    mesh with targets one or two levels up."""
+    from forestfv_public_gb300.mesh import uniform_leaves
+    from forestfv_public_gb300.solver import mesh_adapt, tags_smooth
+    from forestfv_public_gb300.workloads import refine_to_target
+    rng = np.random.default_rng(seed)
+
+    def agree(m, tgt):
+        new, src = mesh_adapt(m, tgt)
+        keep = src >= 0
+        by_src = bool(np.any(tgt[src[keep]] > new.level[keep]))
+        assert by_src == bool(np.any(tgt > m.level + 1))
+        return new, by_src
+
+    leaves = refine_to_target((2, 2, 2), 2, 4, lambda c, h: np.where(c[:, 0] < 0.5, 4, 3))
+    m = Mesh((2, 2, 2), leaves)
+    for _ in range(4):
+        tgt = tags_smooth(m, 7, np.clip(m.level + rng.integers(-2, 4, m.n), 1, 7).astype(np.int32))
+        m, _ = agree(m, tgt)
+    u = Mesh((2, 2, 2), uniform_leaves((2, 2, 2), 3))
+    for up in (1, 2):
+        tgt = u.level.astype(np.int32).copy()
+        pick = rng.choice(u.n, 6, replace=False)
+        tgt[pick] += rng.integers(1, up + 1, 6)
+        tgt[pick[0]] = u.level[pick[0]] + up
+        _, deeper = agree(u, tgt)
+        assert deeper == (up == 2)
