@@ -58,7 +58,10 @@ extern "C" {
 #define FFV_FP32_FLUX 1   /* reconstruction, wave speeds, HLLC in FP32; FP64 residuals,  */
                           /* RK state and stiffened-gas pressure recovery                 */
 
-/* boundary codes, as the reference's fc[].bc (m0_bc.c:3-31) */
+/* boundary codes, as the reference's fc[].bc (m0_bc.c:3-31, m5_bc.c:3-31); every code is
+ * accepted by both models.  Model 5's symmetry face takes the central flux of the cell state
+ * and its mirror image (m5_hllc.c:56-85); its inlet, like the reference's, has no state of its
+ * own (m5_bc.c:35-48: a transmissive face). */
 #define FFV_BC_SYMMETRY 1
 #define FFV_BC_OUTLET 2     /* transmissive */
 #define FFV_BC_INLET 3
