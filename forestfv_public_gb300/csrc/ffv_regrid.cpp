@@ -218,7 +218,6 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
     return true;
   };
 
-  const int64_t chunk = (nn + nth - 1) / (nth ? nth : 1);
   std::vector<std::vector<int32_t>> csub(nth);
   std::vector<int> crc(nth, FFV_OK);
   std::vector<int> tmin(nth, FFV_MAX_LEVEL + 1), tmax(nth, 0);
