@@ -53,3 +53,27 @@ def test_out_of_range_rejected(built_lib):
     with pytest.raises(FFVError):
         Mesh((1, 1, 1), Leaves(np.array([[0, 0, 0]], np.int32), np.array([2], np.int32),
                                np.array([[2, 0, 0]], np.int32)))
+
+
+def test_mesh_leaves_partial_outputs(built_lib):
+    """ffv_mesh_leaves fills any subset of its three outputs (a library-built mesh copies its
+    leaf coordinates only when asked) and refuses a call that asks for none."""
+    import numpy as np
+
+    from forestfv_public_gb300 import _lib
+    from forestfv_public_gb300.mesh import Mesh, uniform_leaves
+    m = Mesh((2, 1, 1), uniform_leaves((2, 1, 1), 3))
+    L = _lib.lib()
+    lev = np.zeros(m.n, np.int32)
+    assert L.ffv_mesh_leaves(m.handle, None, lev.ctypes.data, None) == 0
+    assert np.array_equal(lev, m.level)
+    t = np.zeros((m.n, 3), np.int32)
+    c = np.zeros((m.n, 3), np.int32)
+    assert L.ffv_mesh_leaves(m.handle, t.ctypes.data, None, c.ctypes.data) == 0
+    assert np.array_equal(t, m.tree_ijk) and np.array_equal(c, m.cell_ijk)
+    assert L.ffv_mesh_leaves(m.handle, None, None, None) == 1  # FFV_ERR_ARG
+    wrapped = Mesh.from_handle(m.handle, m.ntrees, m.bc, m.tree_edge)
+    assert np.array_equal(wrapped.level, m.level)
+    assert np.array_equal(wrapped.tree_ijk, m.tree_ijk)
+    assert np.array_equal(wrapped.cell_ijk, m.cell_ijk)
+    wrapped._h = None  # the handle stays owned by m
