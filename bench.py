@@ -18,7 +18,7 @@ One benchmark step is one time step (all RK stages) over the whole mesh; one cel
 is one cell advanced one time step.
 
   value      the metric's form: the FP32-flux form with learned AMR over `steps` steps of
-             the time loop (network every 4 steps, the plain criterion as judge every 8 steps,
+             the time loop (network every step, the plain criterion as judge every 8 steps,
              regrids when it finds cells to refine), CUDA events on the solver's stream
              around the loop (judges and regrids included); state resident in HBM
   plain_fp64_amr  the comparator: plain FP64 with the reference's AMR (meshadaptation
@@ -163,9 +163,10 @@ def wl_config3(small: bool = False, medium: bool = False):
 
 
 AMR_EVERY, AMR_HORIZON, AMR_THRESHOLD = 8, 16, 0.3
-# the network runs every fourth step: a mark predicts a refinement within AMR_HORIZON steps,
-# and the marks accumulate until the next regrid
-AMR_INFER_EVERY = 4
+# the network runs every step, as the learned-indicator configuration specifies (AdaptiveRun
+# takes infer_every > 1 too: a mark predicts a refinement within AMR_HORIZON steps and the
+# marks accumulate until the next regrid)
+AMR_INFER_EVERY = 1
 WALL_LRS = 16
 
 
