@@ -14,6 +14,8 @@ from .build import LIB
 FFV_MAX_MATERIALS = 8
 FFV_FP64 = 0
 FFV_FP32_FLUX = 1
+FFV_FLUX_REFERENCE = 0
+FFV_FLUX_CONSISTENT = 1
 
 ERRORS = {
     0: "ok", 1: "invalid argument", 2: "CUDA runtime error", 3: "mesh description rejected",
@@ -37,7 +39,7 @@ class Params(ctypes.Structure):
                 ("pinf", ctypes.c_double * FFV_MAX_MATERIALS),
                 ("mu", ctypes.c_double * FFV_MAX_MATERIALS),
                 ("amin", ctypes.c_double), ("avf_lim", ctypes.c_double),
-                ("zerou", ctypes.c_int32 * 3), ("reserved1", ctypes.c_int32)]
+                ("zerou", ctypes.c_int32 * 3), ("flux_form", ctypes.c_int32)]
 
 
 class ForestDesc(ctypes.Structure):

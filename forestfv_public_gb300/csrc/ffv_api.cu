@@ -316,6 +316,8 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
   if (p->rk_steps < 1 || p->rk_steps > 4) return FFV_ERR_ARG;
   if (p->precision != FFV_FP64 && p->precision != FFV_FP32_FLUX) return FFV_ERR_ARG;
   if (p->precision != FFV_FP64 && p->model != 5) return FFV_ERR_UNSUPPORTED;
+  if (p->flux_form != FFV_FLUX_REFERENCE && p->flux_form != FFV_FLUX_CONSISTENT) return FFV_ERR_ARG;
+  if (p->flux_form != FFV_FLUX_REFERENCE && p->model != 5) return FFV_ERR_UNSUPPORTED;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0)
     return FFV_ERR_CUDA;
@@ -332,6 +334,7 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
     k.order = p->order;
     k.prelax = p->prelax;
     k.precision = p->precision;
+    k.flux_form = p->flux_form;
     k.nsolids = 0;
     for (int d = 0; d < 3; d++) k.zerou[d] = p->zerou[d];
     for (int i = 0; i < FFV_MAX_MATERIALS; i++) {

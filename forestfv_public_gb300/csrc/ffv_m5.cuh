@@ -9,6 +9,7 @@
 struct M5Consts {
   int nmat, order, prelax, nsolids;
   int precision;  // FFV_FP64 or FFV_FP32_FLUX
+  int flux_form;  // FFV_FLUX_REFERENCE or FFV_FLUX_CONSISTENT
   int zerou[3];
   double gamma[FFV_MAX_MATERIALS], pinf[FFV_MAX_MATERIALS], mu[FFV_MAX_MATERIALS];
   double amin, avf_lim;

@@ -245,8 +245,12 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
   const float vel[3] = {glob<F, 0>(u_S, v_S, w_S), glob<F, 1>(u_S, v_S, w_S),
                         glob<F, 2>(u_S, v_S, w_S)};
   const float re = s.r * s.e;
-  const float Em_S = (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S +
-                      s12_S * v_S + s13_S * w_S) / (r_S * (u_S + SK));
+  const float Em_S =
+      k.flux_form == FFV_FLUX_CONSISTENT
+          ? (re * (uK - SK) - s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
+             s13_S * w_S) / (r_S * (u_S - SK))
+          : (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
+             s13_S * w_S) / (r_S * (u_S + SK));
   float Am[3][3], Al[3][3], AS[3][3], Ag[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -304,7 +308,7 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
 
 // m5_flux.c / m5_flux_gfm.c normal component along face F, FP32
 template <int F, int N>
-__device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, NCf<N> &nc, float *Fn) {
+__device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, bool cons, NCf<N> &nc, float *Fn) {
   using C = K5<N>;
   constexpr int a = Fr<F, 0>::ax, sg = Fr<F, 0>::sg;
   const float vu = gfm ? s.ut : s.u, vv = gfm ? s.vt : s.v, vw = gfm ? s.wt : s.w;
@@ -314,7 +318,8 @@ __device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, NCf<N> &nc, float
   for (int v = 0; v < N; v++) Fn[C::i0 + v] = sgn<sg>(va * s.ra[v]);
 #pragma unroll
   for (int b = 0; b < 3; b++)
-    Fn[C::i1 + b] = sgn<sg>(gfm ? va * vel[b] * s.r - s.st[b][a] : va * vel[b] * s.r + s.st[b][a]);
+    Fn[C::i1 + b] = sgn<sg>((gfm || cons) ? va * vel[b] * s.r - s.st[b][a]
+                                          : va * vel[b] * s.r + s.st[b][a]);
   Fn[C::i2] = sgn<sg>(s.r * s.e * va - s.st[a][0] * vu - s.st[a][1] * vv - s.st[a][2] * vw);
   if (flag == 0 || flag == 3) {
 #pragma unroll
@@ -324,7 +329,7 @@ __device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, NCf<N> &nc, float
 #pragma unroll
     for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
 #pragma unroll
-    for (int q = 0; q < 9; q++) nc.A[q] = gfm ? s.A[q] : -s.A[q];
+    for (int q = 0; q < 9; q++) nc.A[q] = (gfm || cons) ? s.A[q] : -s.A[q];
   } else if (flag == 4) {  // symmetry face (m5_flux.c:58-66): the velocity is the caller's
 #pragma unroll
     for (int v = 0; v < N - 1; ++v) nc.avf[v] = s.avf[v];
@@ -383,19 +388,19 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
   const bool left_star = gfm ? (SL < 0.0f && 0.0f <= u_S) : (SL <= 0.0f && 0.0f <= u_S);
   const bool right_star = gfm ? (u_S < 0.0f && 0.0f < SR) : (u_S <= 0.0f && 0.0f <= SR);
   if (0.0f <= SL) {
-    flux_n_f<F>(L, 0, gfm, nc, Fn);
+    flux_n_f<F>(L, 0, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
   } else if (left_star) {
     st |= star_region_f<F>(k, L, L, R, true, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
-    flux_n_f<F>(L, 1, gfm, nc, Fn);
+    flux_n_f<F>(L, 1, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
 #pragma unroll
     for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SL * (Us[iv] - L.vec[iv]);
   } else if (right_star) {
     st |= star_region_f<F>(k, R, L, R, false, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
-    flux_n_f<F>(R, 2, gfm, nc, Fn);
+    flux_n_f<F>(R, 2, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
 #pragma unroll
     for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SR * (Us[iv] - R.vec[iv]);
   } else if (SR <= 0.0f) {
-    flux_n_f<F>(R, 3, gfm, nc, Fn);
+    flux_n_f<F>(R, 3, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
   } else {
     st |= FFV_ST_NO_BRANCH;
 #pragma unroll
@@ -413,7 +418,7 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
 // m5_hllc.c:56-85 in FP32, a symmetry face: the mean of the physical fluxes of the cell's own
 // state and of its mirror image, advected terms moving with the mean velocity, no HLLC part
 template <int F, int N>
-__device__ void symmetry_acc_f(const SolF<N> &Lc, float Area, float *ff, float unc[3]) {
+__device__ void symmetry_acc_f(const SolF<N> &Lc, bool cons, float Area, float *ff, float unc[3]) {
   using C = K5<N>;
   SolF<N> Rc;
   ghost_f<F, N>(Lc, 1, Rc);
@@ -422,8 +427,8 @@ __device__ void symmetry_acc_f(const SolF<N> &Lc, float Area, float *ff, float u
   nc.unc[1] = 0.5f * (Lc.v + Rc.v);
   nc.unc[2] = 0.5f * (Lc.w + Rc.w);
   float FL[C::NEQ], FR[C::NEQ];
-  flux_n_f<F>(Lc, 4, false, nc, FL);
-  flux_n_f<F>(Rc, 4, false, nc, FR);
+  flux_n_f<F>(Lc, 4, false, cons, nc, FL);
+  flux_n_f<F>(Rc, 4, false, cons, nc, FR);
 #pragma unroll
   for (int iv = 0; iv < C::NEQ; ++iv) ff[iv] += Area * ((0.5f * FL[iv]) + (0.5f * FR[iv]));
 #pragma unroll
@@ -1019,7 +1024,7 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
   if (kind == (FFV_FK_BC | FFV_BC_SYMMETRY)) {  // the cell's own state (m5_hllc.c:59-63)
     record_of_cell<N>(k, S, m.n, c, U);
     make_sol_f<N>(k, U, 0.0f, L);
-    symmetry_acc_f<F, N>(L, (float)g.area[l], ff, uf);
+    symmetry_acc_f<F, N>(L, k.flux_form == FFV_FLUX_CONSISTENT, (float)g.area[l], ff, uf);
     return;
   }
   if (k.order == 2) load_record<N>(SF, m.n, F, c, U);

@@ -243,8 +243,14 @@ __device__ unsigned star_region(const M5Consts &k, const Sol<N> &s, const Sol<N>
   const double vel[3] = {glob<F, 0>(u_S, v_S, w_S), glob<F, 1>(u_S, v_S, w_S),
                          glob<F, 2>(u_S, v_S, w_S)};
   const double re = s.r * s.e;
-  const double Em_S = (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S +
-                       s12_S * v_S + s13_S * w_S) / (r_S * (u_S + SK));
+  // the reference's expression, or the Rankine-Hugoniot energy jump across the S_K wave
+  // (FFV_FLUX_CONSISTENT, include/ffv.h)
+  const double Em_S =
+      k.flux_form == FFV_FLUX_CONSISTENT
+          ? (re * (uK - SK) - s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
+             s13_S * w_S) / (r_S * (u_S - SK))
+          : (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
+             s13_S * w_S) / (r_S * (u_S + SK));
   double Am[3][3], Al[3][3], AS[3][3], Ag[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -302,7 +308,7 @@ __device__ unsigned star_region(const M5Consts &k, const Sol<N> &s, const Sol<N>
 // m5_flux.c (gfm false) / m5_flux_gfm.c (gfm true), normal component along face F:
 // Fn[iv] = sum_d F[iv][d] n_d with n the signed unit axis of F.
 template <int F, int N>
-__device__ void flux_n(const Sol<N> &s, int flag, bool gfm, NC<N> &nc, double *Fn) {
+__device__ void flux_n(const Sol<N> &s, int flag, bool gfm, bool cons, NC<N> &nc, double *Fn) {
   using C = K5<N>;
   constexpr int a = Fr<F, 0>::ax, sg = Fr<F, 0>::sg;
   const double vu = gfm ? s.ut : s.u, vv = gfm ? s.vt : s.v, vw = gfm ? s.wt : s.w;
@@ -312,7 +318,8 @@ __device__ void flux_n(const Sol<N> &s, int flag, bool gfm, NC<N> &nc, double *F
   for (int v = 0; v < N; v++) Fn[C::i0 + v] = sgn<sg>(va * s.ra[v]);
 #pragma unroll
   for (int b = 0; b < 3; b++)
-    Fn[C::i1 + b] = sgn<sg>(gfm ? va * vel[b] * s.r - s.st[b][a] : va * vel[b] * s.r + s.st[b][a]);
+    Fn[C::i1 + b] = sgn<sg>((gfm || cons) ? va * vel[b] * s.r - s.st[b][a]
+                                          : va * vel[b] * s.r + s.st[b][a]);
   Fn[C::i2] = sgn<sg>(s.r * s.e * va - s.st[a][0] * vu - s.st[a][1] * vv - s.st[a][2] * vw);
   if (flag == 0 || flag == 3) {
 #pragma unroll
@@ -322,7 +329,7 @@ __device__ void flux_n(const Sol<N> &s, int flag, bool gfm, NC<N> &nc, double *F
 #pragma unroll
     for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
 #pragma unroll
-    for (int q = 0; q < 9; q++) nc.A[q] = gfm ? s.A[q] : -s.A[q];
+    for (int q = 0; q < 9; q++) nc.A[q] = (gfm || cons) ? s.A[q] : -s.A[q];
   } else if (flag == 4) {  // symmetry face (m5_flux.c:58-66): the velocity is the caller's
 #pragma unroll
     for (int v = 0; v < N - 1; ++v) nc.avf[v] = s.avf[v];
@@ -385,19 +392,19 @@ __device__ unsigned hllc_acc(const M5Consts &k, Sol<N> L, Sol<N> R, int bc, bool
   const bool left_star = gfm ? (SL < 0.0 && 0.0 <= u_S) : (SL <= 0.0 && 0.0 <= u_S);
   const bool right_star = gfm ? (u_S < 0.0 && 0.0 < SR) : (u_S <= 0.0 && 0.0 <= SR);
   if (0.0 <= SL) {
-    flux_n<F>(L, 0, gfm, nc, Fn);
+    flux_n<F>(L, 0, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
   } else if (left_star) {
     st |= star_region<F>(k, L, L, R, true, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
-    flux_n<F>(L, 1, gfm, nc, Fn);
+    flux_n<F>(L, 1, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
 #pragma unroll
     for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SL * (Us[iv] - L.vec[iv]);
   } else if (right_star) {
     st |= star_region<F>(k, R, L, R, false, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
-    flux_n<F>(R, 2, gfm, nc, Fn);
+    flux_n<F>(R, 2, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
 #pragma unroll
     for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SR * (Us[iv] - R.vec[iv]);
   } else if (SR <= 0.0) {
-    flux_n<F>(R, 3, gfm, nc, Fn);
+    flux_n<F>(R, 3, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
   } else {
     st |= FFV_ST_NO_BRANCH;
 #pragma unroll
@@ -418,7 +425,7 @@ __device__ unsigned hllc_acc(const M5Consts &k, Sol<N> L, Sol<N> R, int bc, bool
 // (m5_bc_symmetry: normal velocity reversed), the advected volume fractions, energies and
 // deformation moving with the mean velocity, no HLLC part; accumulated as m5_residual.c:155-165
 template <int F, int N>
-__device__ void symmetry_acc(const Sol<N> &Lc, double Area, double *ff, double unc[3]) {
+__device__ void symmetry_acc(const Sol<N> &Lc, bool cons, double Area, double *ff, double unc[3]) {
   using C = K5<N>;
   Sol<N> Rc;
   ghost<F, N>(Lc, 1, Rc);
@@ -427,8 +434,8 @@ __device__ void symmetry_acc(const Sol<N> &Lc, double Area, double *ff, double u
   nc.unc[1] = 0.5 * (Lc.v + Rc.v);
   nc.unc[2] = 0.5 * (Lc.w + Rc.w);
   double FL[C::NEQ], FR[C::NEQ];
-  flux_n<F>(Lc, 4, false, nc, FL);
-  flux_n<F>(Rc, 4, false, nc, FR);
+  flux_n<F>(Lc, 4, false, cons, nc, FL);
+  flux_n<F>(Rc, 4, false, cons, nc, FR);
 #pragma unroll
   for (int iv = 0; iv < C::NEQ; ++iv) ff[iv] += (Area) * ((0.5 * FL[iv]) + (0.5 * FR[iv]));
 #pragma unroll
@@ -799,7 +806,7 @@ __device__ void face_flux(const ffv_dmesh &m, const ffv_geom &g, const M5Consts 
     // the cell's own state, not the face state; the HLLC flux the reference computes first
     // for this face is discarded (m5_hllc.c:59-63)
     make_sol<N>(k, Sc, Sc, false, L);
-    symmetry_acc<F, N>(L, g.area[l], ff, uf);
+    symmetry_acc<F, N>(L, k.flux_form == FFV_FLUX_CONSISTENT, g.area[l], ff, uf);
     return;
   }
   if (k.order == 2) load_face_state<N>(SF, m.n, F, c, U);

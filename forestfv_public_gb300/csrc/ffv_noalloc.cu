@@ -16,8 +16,17 @@
 // streams, or different host threads without ordering) race on the array.
 //
 // Set-up: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; that first call should
-// come before any stream capture on the device.
+// cudaGetSymbolAddress (with that device current) and caches it together with the id of the
+// device's current CUDA context; a later call in another context (after cudaDeviceReset, or
+// a reset of the primary context, reloads the module, possibly at another address) looks
+// the address up again.  With lazy module loading (CUDA_MODULE_LOADING=LAZY, the default)
+// that first lookup is also what loads this library's module on the device and reserves the
+// array, so it can fail for lack of device memory (FFV_ERR_CUDA).  A caller with a fixed
+// memory budget makes its first call -- or sets CUDA_MODULE_LOADING=EAGER -- before it takes
+// the rest of the device's memory, and outside any stream capture on that device.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <mutex>
 
 #include "ffv_device.cuh"
@@ -49,7 +58,9 @@ static_assert(sizeof(int32_t) * 6 * kMaxCells <= kOffSN - kOffSF, "staging fits"
 static __device__ __align__(256) unsigned char ffv_noalloc_scratch[kBytes];
 
 std::mutex g_mu;
-unsigned char *g_base[kMaxDevices];  // device address of the array, per device (set-up)
+// device address of the array per device, and the id of the context it was looked up in
+unsigned char *g_base[kMaxDevices];
+unsigned long long g_ctx[kMaxDevices];
 
 // [n][6] -> [6][n], the device layout of the neighbour slots
 __global__ void noalloc_nbr_face_major(const int32_t *__restrict__ raw, int32_t *__restrict__ out,
@@ -66,15 +77,39 @@ __global__ void noalloc_begin(double *dt_slot, double dt, unsigned *status) {
   *status = 0u;
 }
 
+// id of the current context (cuCtxGetId through the runtime's driver entry point, so that the
+// library needs no link against the driver library); false when it cannot be had
+bool current_context_id(unsigned long long *id) {
+  static PFN_cuCtxGetId_v12000 fn = [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return (PFN_cuCtxGetId_v12000)f;
+  }();
+  return fn && fn(nullptr, id) == CUDA_SUCCESS;
+}
+
 int base_for_current_device(unsigned char **out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess) return FFV_ERR_CUDA;
   if (dev < 0 || dev >= kMaxDevices) return FFV_ERR_UNSUPPORTED;
+  // makes the device's primary context current (the runtime creates it here if needed)
+  if (cudaSetDevice(dev) != cudaSuccess) return FFV_ERR_CUDA;
+  unsigned long long ctx = 0;
+  const bool have_ctx = current_context_id(&ctx);
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_base[dev]) {
+  if (!g_base[dev] || !have_ctx || g_ctx[dev] != ctx) {
     void *p = nullptr;
-    if (cudaGetSymbolAddress(&p, ffv_noalloc_scratch) != cudaSuccess || !p) return FFV_ERR_CUDA;
+    if (cudaGetSymbolAddress(&p, ffv_noalloc_scratch) != cudaSuccess || !p) {
+      cudaGetLastError();
+      g_base[dev] = nullptr;
+      return FFV_ERR_CUDA;
+    }
     g_base[dev] = (unsigned char *)p;
+    g_ctx[dev] = have_ctx ? ctx : 0;
   }
   *out = g_base[dev];
   return FFV_OK;

@@ -52,6 +52,15 @@ def bubble_config2(lmin: int = 4, lmax: int = 8, band_cells: float = 22.0, seed:
     with tanh in volume fraction, radius perturbed by seeded harmonics l <= 8 of relative
     amplitude 1e-3; 2^3 trees, levels lmin..lmax refined around the interface.
     Returns (Mesh, S [neq, n], params)."""
+    leaves, state = bubble_config2_parts(lmin, lmax, band_cells, seed, radius)
+    mesh = Mesh((2, 2, 2), leaves)
+    return mesh, state(mesh.centroids()), dict(BUBBLE)
+
+
+def bubble_config2_parts(lmin: int = 4, lmax: int = 8, band_cells: float = 22.0,
+                         seed: int = 20261203, radius: float = 0.1):
+    """bubble_config2 without the face tables: its leaves (2^3 trees) and the function
+    from cell centroids to the initial state (numpy only)."""
     c0 = np.array([0.5, 0.5, 0.5])
     hmin = 0.5 / (1 << (lmax - 1))
     coeff_rng = np.random.default_rng(seed + 1)
@@ -77,17 +86,16 @@ def bubble_config2(lmin: int = 4, lmax: int = 8, band_cells: float = 22.0, seed:
         lev = lmax - np.floor(np.maximum(d, 0.0) / (band_cells * hmin * 2.0)).astype(np.int64)
         return np.maximum(lev, lmin)
 
-    leaves = refine_to_target((2, 2, 2), lmin, lmax, target)
-    mesh = Mesh((2, 2, 2), leaves)
-    x = mesh.centroids()
-    w = 2.0 * hmin
-    r = np.linalg.norm(x - c0, axis=1)
-    R = np.full_like(r, radius)
-    near = np.abs(r - radius) < 20.0 * w  # the tanh profile is saturated beyond this
-    r[near], R[near] = radius_at(x[near])
-    a_gas = 0.5 * (1.0 - np.tanh((r - R) / w))
-    S = mixture_state(BUBBLE, a_gas)
-    return mesh, S, dict(BUBBLE)
+    def state(x):
+        w = 2.0 * hmin
+        r = np.linalg.norm(x - c0, axis=1)
+        R = np.full_like(r, radius)
+        near = np.abs(r - radius) < 20.0 * w  # the tanh profile is saturated beyond this
+        r[near], R[near] = radius_at(x[near])
+        a_gas = 0.5 * (1.0 - np.tanh((r - R) / w))
+        return mixture_state(BUBBLE, a_gas)
+
+    return refine_to_target((2, 2, 2), lmin, lmax, target), state
 
 
 def mixture_state(mat: dict, a_gas: np.ndarray) -> np.ndarray:
@@ -126,6 +134,15 @@ def bubble_wall_config3(lmin: int = 4, lmax: int = 9, band_cells: float = 6.5,
     (9.9 M cells at the default sizes).  The solid cells take the reference's m5_init_S
     state (init_S.c:205-266: the cell's material at 1 - 2 AMIN, the others at AMIN,
     deformation A = I; A = 0 in fluid cells).  Returns (Mesh, S [21, n], params)."""
+    leaves, state = bubble_wall_parts(lmin, lmax, band_cells, radius, standoff, wall_z)
+    mesh = Mesh((2, 2, 2), leaves)
+    return mesh, state(mesh.centroids()), dict(WALL)
+
+
+def bubble_wall_parts(lmin: int = 4, lmax: int = 9, band_cells: float = 6.5,
+                      radius: float = 0.1, standoff: float = 1.5, wall_z: float = 0.2):
+    """bubble_wall_config3 without the face tables: its leaves (2^3 trees) and the
+    function from cell centroids to the initial state (numpy only)."""
     c0 = np.array([0.5, 0.5, wall_z + standoff * radius])
     hmin = 0.5 / (1 << (lmax - 1))
 
@@ -135,13 +152,12 @@ def bubble_wall_config3(lmin: int = 4, lmax: int = 9, band_cells: float = 6.5,
         lev = lmax - np.floor(np.maximum(d, 0.0) / (band_cells * hmin * 2.0)).astype(np.int64)
         return np.maximum(lev, lmin)
 
-    leaves = refine_to_target((2, 2, 2), lmin, lmax, target)
-    mesh = Mesh((2, 2, 2), leaves)
-    x = mesh.centroids()
-    r = np.linalg.norm(x - c0, axis=1)
-    a_gas = 0.5 * (1.0 - np.tanh((r - radius) / (2.0 * hmin)))
-    S = wall_state(WALL, x[:, 2] < wall_z, a_gas)
-    return mesh, S, dict(WALL)
+    def state(x):
+        r = np.linalg.norm(x - c0, axis=1)
+        a_gas = 0.5 * (1.0 - np.tanh((r - radius) / (2.0 * hmin)))
+        return wall_state(WALL, x[:, 2] < wall_z, a_gas)
+
+    return refine_to_target((2, 2, 2), lmin, lmax, target), state
 
 
 def wall_state(mat: dict, solid: np.ndarray, a_gas: np.ndarray) -> np.ndarray:

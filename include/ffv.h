@@ -58,6 +58,31 @@ extern "C" {
 #define FFV_FP32_FLUX 1   /* reconstruction, wave speeds, HLLC in FP32; FP64 residuals,  */
                           /* RK state and stiffened-gas pressure recovery                 */
 
+/* Model 5's flux, as the reference writes it or made consistent (ffv_params.flux_form).
+ * FFV_FLUX_REFERENCE is the reference's m5 flux to the last bit.  Three of its expressions
+ * disagree with the rest of its own HLLC solver:
+ *   - the star-state energy (m5_star_region.c:59),
+ *       (rho E)* = (rho E_K (u_K - S_K) + s11_K u_K - s12_K v_K - s13_K w_K + sigma* . u*)
+ *                  / (u* + S_K),
+ *     gives (rho E)* = -rho E at u* = 0: every face at rest carries a spurious energy flux of
+ *     about 2 c rho E, which boundary faces and material interfaces feed into the solution;
+ *   - m5_flux.c:20-34 takes the momentum flux as rho u u + sigma, while m5_flux_gfm.c:20-34,
+ *     the contact speed (m5_wave_speeds.c) and model 0 (m0_flux.c: rho u u + p) all have
+ *     rho u u - sigma with the Cauchy stress sigma = -p I + deviator: the fluid is pushed by
+ *     the negated pressure;
+ *   - m5_flux.c:53-56 advects the deformation tensor of the left and right states negated
+ *     (-A) where m5_flux_gfm.c and the star states take +A.
+ * On these the reference's model-5 scheme stops with a NaN wave speed after one step of
+ * Sod's problem, and amplifies rounding-level differences by ~1e9 within 20 steps of the
+ * bubble configurations.  FFV_FLUX_CONSISTENT (a deliberate deviation, off by default)
+ * takes the Rankine-Hugoniot energy jump across the S_K wave with the normal energy flux
+ * rho E u - sigma_n . u,
+ *       (rho E)* = (rho E_K (u_K - S_K) - sigma_K . u_K + sigma* . u*) / (u* - S_K),
+ * and m5_flux_gfm.c's signs in m5_flux.c (rho u u - sigma, +A); with it model 5 reproduces
+ * model 0's solution of Sod's problem. */
+#define FFV_FLUX_REFERENCE 0
+#define FFV_FLUX_CONSISTENT 1
+
 /* boundary codes, as the reference's fc[].bc (m0_bc.c:3-31, m5_bc.c:3-31); every code is
  * accepted by both models.  Model 5's symmetry face takes the central flux of the cell state
  * and its mirror image (m5_hllc.c:56-85); its inlet, like the reference's, has no state of its
@@ -83,7 +108,7 @@ typedef struct ffv_params {
   double amin;          /* model 5: AMIN, volume-fraction floor */
   double avf_lim;       /* model 5: AVF_LIM, solid-fraction level of the ghost-fluid interface */
   int32_t zerou[3];     /* model 5: ZEROU0..2 (freeze a velocity component, m5_RK.c:93-122) */
-  int32_t reserved1;
+  int32_t flux_form;    /* model 5: FFV_FLUX_REFERENCE (0, default) or FFV_FLUX_CONSISTENT */
 } ffv_params;
 
 /* A Cartesian forest: ntrees[0] x ntrees[1] x ntrees[2] cubic hex trees of edge
@@ -318,7 +343,12 @@ const char *ffv_error_string(int code);
  * share the array and it keeps the last call's contents (each call rewrites what it
  * reads and clears its status word first); calls whose work overlaps on the GPU race on
  * it.  The first call on a device looks up the array's address (cudaGetSymbolAddress) and
- * should come before any stream capture on that device. */
+ * should come before any stream capture on that device; the address is cached per device
+ * together with the id of the CUDA context it belongs to, and looked up again in a new
+ * context (after cudaDeviceReset).  With lazy module loading (CUDA_MODULE_LOADING=LAZY, the
+ * default) that first lookup also loads the library's module and reserves the array, so it
+ * can fail for lack of device memory (FFV_ERR_CUDA): a caller with a fixed budget makes its
+ * first call, or sets CUDA_MODULE_LOADING=EAGER, before it takes the rest of the memory. */
 #define FFV_NOALLOC_MAX_CELLS 65536
 #define FFV_NOALLOC_SCRATCH_BYTES 21758464
 int ffv_step_noalloc(const ffv_mesh *m, const ffv_params *p, double *d_S, double dt,

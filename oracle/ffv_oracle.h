@@ -58,7 +58,10 @@ typedef struct ffvo_m5_params {
   int32_t rk_steps;  /* RK_STEPS */
   int32_t prelax;    /* PRELAX: 1 (two materials, closed form) or 3 (iterative) */
   int32_t zerou[3];  /* ZEROU0..2 */
-  int32_t reserved;
+  int32_t flux_form;   /* 0: the reference's m5 flux, as written; 1: the consistent flux (a
+                          deviation): the Rankine-Hugoniot star-state energy in place of
+                          m5_star_region.c:59, and m5_flux.c's momentum flux and left/right
+                          deformation flux with m5_flux_gfm.c's signs (rho u u - sigma, +A) */
   double gamma[4], pinf[4], mu[4];  /* MATERGAMA, MATERPINF, MATERMUSH */
   double amin;       /* AMIN */
   double avf_lim;    /* AVF_LIM */

@@ -23,6 +23,7 @@
 typedef struct cfg {
   int N, neq, ncons, i0, i1, i2, i3, i4, i5, order, rk_steps, prelax, nsolids;
   int zerou[3];
+  int flux_form;
   double gamma[MAXN], pinf[MAXN], mu[MAXN], amin, avf_lim, dt;
   double lim[MAXNEQ];
 } cfg;
@@ -270,8 +271,17 @@ static int star_region(const cfg *k, const geo *g, const sol *s, const sol *L, c
   double vel[3];
   for (int d = 0; d < 3; d++) vel[d] = u_S * g->n[d] + v_S * g->t1[d] + w_S * g->t2[d];
   double re = s->r * s->e;
-  double Em_S = (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
-                 s13_S * w_S) / (r_S * (u_S + SK));
+  double Em_S;
+  if (k->flux_form) {
+    /* energy jump across the S_K wave, S_K (U*_K - U_K) = F*_K - F_K, with the normal energy
+       flux rho E u - sigma_n . u: (rho E)* (u* - S_K) = rho E (u_K - S_K) - sigma_K . u_K +
+       sigma* . u* */
+    Em_S = (re * (uK - SK) - s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
+            s13_S * w_S) / (r_S * (u_S - SK));
+  } else {
+    Em_S = (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
+            s13_S * w_S) / (r_S * (u_S + SK));
+  }
   double Rm[3][3], Rt[3][3], Am[3][3], Al[3][3], AS[3][3], Ag[3][3];
   frame_rows(g, Rm);
   for (int i = 0; i < 3; i++)
@@ -327,15 +337,15 @@ static void phys_flux(const cfg *k, const sol *s, int flag, int gfm, ncs *nc, do
     for (int d = 0; d < 3; d++) F[k->i0 + v][d] = vel[d] * s->ra[v];
   for (int a = 0; a < 3; a++)
     for (int d = 0; d < 3; d++)
-      F[k->i1 + a][d] = gfm ? vel[d] * vel[a] * s->r - s->st[a][d]
-                            : vel[d] * vel[a] * s->r + s->st[a][d];
+      F[k->i1 + a][d] = (gfm || k->flux_form) ? vel[d] * vel[a] * s->r - s->st[a][d]
+                                              : vel[d] * vel[a] * s->r + s->st[a][d];
   for (int d = 0; d < 3; d++)
     F[k->i2][d] = s->r * s->e * vel[d] - s->st[d][0] * vu - s->st[d][1] * vv - s->st[d][2] * vw;
   if (flag == 0 || flag == 3) {
     for (int d = 0; d < 3; d++) nc->unc[d] = vel[d];
     for (int v = 0; v < N - 1; ++v) nc->avf[v] = s->avf[v];
     for (int v = 0; v < N; ++v) nc->are[v] = s->are[v];
-    for (int q = 0; q < 9; q++) nc->A[q] = gfm ? s->A[q] : -s->A[q];
+    for (int q = 0; q < 9; q++) nc->A[q] = (gfm || k->flux_form) ? s->A[q] : -s->A[q];
   } else if (flag == 4) { /* symmetry face: the caller gives the velocity */
     for (int v = 0; v < N - 1; ++v) nc->avf[v] = s->avf[v];
     for (int v = 0; v < N; ++v) nc->are[v] = s->are[v];
@@ -1032,6 +1042,8 @@ static int make_cfg(const ffvo_m5_params *p, double dt, cfg *k) {
   k->order = p->order;
   k->rk_steps = p->rk_steps;
   k->prelax = p->prelax;
+  k->flux_form = p->flux_form;
+  if (k->flux_form != 0 && k->flux_form != 1) return 10;
   for (int d = 0; d < 3; d++) k->zerou[d] = p->zerou[d];
   for (int i = 0; i < N; i++) {
     k->gamma[i] = p->gamma[i];

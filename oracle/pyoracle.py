@@ -30,7 +30,7 @@ class _Params(ctypes.Structure):
 class _M5Params(ctypes.Structure):
     _fields_ = [("nmat", ctypes.c_int32), ("order", ctypes.c_int32), ("rk_steps", ctypes.c_int32),
                 ("prelax", ctypes.c_int32), ("zerou", ctypes.c_int32 * 3),
-                ("reserved", ctypes.c_int32), ("gamma", ctypes.c_double * 4),
+                ("flux_form", ctypes.c_int32), ("gamma", ctypes.c_double * 4),
                 ("pinf", ctypes.c_double * 4), ("mu", ctypes.c_double * 4),
                 ("amin", ctypes.c_double), ("avf_lim", ctypes.c_double)]
 
@@ -103,7 +103,7 @@ def m5_advance(mesh: OracleMesh, S_aos: np.ndarray, dt: float, nsteps: int, m5: 
     """Model 5: advance an AoS [n, 3N+12] state; returns the new state."""
     S = np.ascontiguousarray(S_aos, dtype=np.float64).copy()
     p = _M5Params(nmat=len(m5["gamma"]), order=order, rk_steps=rk_steps, prelax=m5["prelax"],
-                  amin=m5["amin"], avf_lim=m5["avf_lim"])
+                  amin=m5["amin"], avf_lim=m5["avf_lim"], flux_form=m5.get("flux_form", 0))
     p.zerou[:] = zerou
     for i, (g, q, mu) in enumerate(zip(m5["gamma"], m5["pinf"], m5["mu"])):
         p.gamma[i], p.pinf[i], p.mu[i] = g, q, mu
