@@ -80,31 +80,70 @@ def _bubble_solver_kwargs(p):
                 amin=p["amin"], avf_lim=1.0, prelax=3)
 
 
-def wl_config2(small: bool = False, medium: bool = False):
+def _wall_solver_kwargs(p):
+    return dict(model=5, order=2, rk_steps=2, gamma=p["gamma"], pinf=p["pinf"], mu=p["mu"],
+                amin=p["amin"], avf_lim=p["avf_lim"], prelax=3)
+
+
+C_SOLID = float(np.sqrt(3.5 * (5e6 + 3.2e10) / 2700.0))
+# (lmax, refinement band in finest cells): full size, medium (profiler captures), small
+WALL_SIZES = {"config3": (9, 6.5), "config3m": (7, 4.0), "config3s": (5, 2.0)}
+# (lmin, lmax, band)
+BUBBLE_SIZES = {"config2": (4, 8, 22.0), "config2m": (4, 7, 12.0), "config2s": (4, 6, 2.0)}
+FLUX_FORMS = {"reference": 0, "consistent": 1}
+FLUX_FORM_NOTE = {
+    0: "the reference's m5 flux as written (m5_star_region.c:59, m5_flux.c:20-34, 53-56)",
+    1: "consistent: Rankine-Hugoniot star-state energy and m5_flux_gfm.c's momentum and "
+       "deformation signs in m5_flux.c (a deviation from the reference, FFV_FLUX_CONSISTENT)"}
+
+
+def workload_config(workload: str, n: int | None = None, levels=None) -> dict:
+    """The static description of a workload, the same for both arms (the counts from the
+    mesh as generated, before any adaptation)."""
+    if n is None:
+        F = cpu_case(workload)[0]
+        n, levels = F.n, sorted(int(x) for x in np.unique(F.level))
+    if workload == "config1":
+        return {"workload": "config1 Sod 32^3, model 0, plain FP64, MUSCL-HLLC, RK2, CFL 0.4",
+                "cells": n, "trees": [4, 4, 4], "level": 4, "dt": float(0.4 / 32.0 / np.sqrt(1.4)),
+                "parallelism": "single GPU",
+                "l2": "flushed between timed steps (256 MiB write); state 1.3 MB < L2"}
+    if workload.startswith("config3"):
+        lmax = WALL_SIZES[workload][0]
+        size = {"config3": "", "config3m": " (medium size)", "config3s": " (small size)"}[workload]
+        return {"workload": f"config3 bubble collapse near a hyperelastic wall{size}, model 5 "
+                            f"(3 materials), levels 4-{lmax} AMR; FP32-flux + learned AMR against "
+                            "plain FP64 + AMR; MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
+                "cells": n, "levels": levels, "neq": 21,
+                "dt": 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": 0.01,
+                "cfl_speed": "solid sound speed, finest cell", "parallelism": "single GPU",
+                "l2": f"state {8 * 21 * n / 1e6:.0f} MB > L2 (129 MB): no flush needed"}
+    lmin, lmax, _ = BUBBLE_SIZES[workload]
+    size = {"config2": "", "config2m": " (medium size)", "config2s": " (small size)"}[workload]
+    return {"workload": f"config2 bubble collapse in liquid{size}, model 5 (2 materials), levels "
+                        f"{lmin}-{lmax} AMR, plain FP64 and FP32-flux forms, MUSCL-HLLC, PRELAX 3, RK2",
+            "cells": n, "levels": levels, "neq": 18,
+            "dt": 0.01 * (0.5 / (1 << (lmax - 1))) / C_LIQUID, "cfl": 0.01,
+            "parallelism": "single GPU",
+            "l2": f"state {8 * 18 * n / 1e6:.0f} MB > L2 (129 MB): no flush needed"}
+
+
+def _config2(name: str):
     from forestfv_public_gb300 import workloads as W
-    if small:  # CPU sample: same physics, levels 4..6
-        mesh, S0, p = W.bubble_config2(lmin=4, lmax=6, band_cells=2.0)
-        hmin = 0.5 / (1 << 5)
-    elif medium:  # profiler captures: levels 4..7, 0.36 M cells
-        mesh, S0, p = W.bubble_config2(lmin=4, lmax=7, band_cells=12.0)
-        hmin = 0.5 / (1 << 6)
-    else:
-        mesh, S0, p = W.bubble_config2()
-        hmin = 0.5 / (1 << 7)
-    dt = 0.01 * hmin / C_LIQUID
-    neq = S0.shape[0]
-    cfg = {"workload": "config2 bubble collapse in liquid, model 5 (2 materials), levels 5-8 AMR, "
-                       "plain FP64, MUSCL-HLLC, PRELAX 3, RK2",
-           "cells": int(mesh.n), "levels": sorted(int(x) for x in np.unique(mesh.level)),
-           "neq": neq, "dt": float(dt), "cfl": 0.01, "parallelism": "single GPU",
-           "l2": "state 331 MB > L2 (129 MB): no flush needed"}
-    # algorithmic bytes per cell of each kernel (compulsory traffic, neighbour re-reads excluded)
-    d = 8 * neq
-    alg = {"m5_recon_face": d + 28 + 6 * d,
-           "m5_face_flux": 6 * d + d + 28 + 6 * d + 6 * 3 * 8 + 6 * 8,
-           "m5_cell_update": d + 6 * d + 6 * 3 * 8 + d + 28 + d + d + 1,
-           "m5_relax_cell": d + d + 1}
-    return mesh, S0, dt, cfg, _bubble_solver_kwargs(p), alg, False
+    lmin, lmax, band = BUBBLE_SIZES[name]
+    mesh, S0, p = W.bubble_config2(lmin=lmin, lmax=lmax, band_cells=band)
+    cfg = workload_config(name, int(mesh.n), sorted(int(x) for x in np.unique(mesh.level)))
+    alg = m5_alg_bytes(S0.shape[0], 2)
+    return mesh, S0, cfg["dt"], cfg, _bubble_solver_kwargs(p), alg, False
+
+
+def wl_config2(small: bool = False, medium: bool = False):
+    return _config2("config2s" if small else "config2m" if medium else "config2")
+
+
+def wl_config2m(small: bool = False):
+    """config2 physics on a 0.36 M-cell mesh (levels 4-7): the size profiler captures use."""
+    return _config2("config2s" if small else "config2m")
 
 
 def wl_config1(small: bool = False):
@@ -112,57 +151,32 @@ def wl_config1(small: bool = False):
     trees, level = (4, 4, 4), 4
     mesh = Mesh(trees, uniform_leaves(trees, level))
     S0 = sod_state(mesh.centroids())
-    dt = 0.4 * (1.0 / 32.0) / np.sqrt(1.4)
-    cfg = {"workload": "config1 Sod 32^3, model 0, plain FP64, MUSCL-HLLC, RK2, CFL 0.4",
-           "cells": int(mesh.n), "trees": list(trees), "level": level, "dt": float(dt),
-           "parallelism": "single GPU",
-           "l2": "flushed between timed steps (256 MiB write); state 1.3 MB < L2"}
+    cfg = workload_config("config1", int(mesh.n), [level])
     alg = {"m0_recon": 40 + 28 + 240, "m0_flux_rk<2>": 240 + 40 + 40 + 28 + 40}
-    return mesh, S0, float(dt), cfg, dict(model=0), alg, True
+    return mesh, S0, cfg["dt"], cfg, dict(model=0), alg, True
 
 
-def wl_config2m(small: bool = False):
-    """config2 physics on a 0.36 M-cell mesh (levels 4-7): the size profiler captures use."""
-    out = wl_config2(small=small, medium=not small)
-    out[3]["workload"] = out[3]["workload"].replace("levels 5-8", "levels 4-7 (medium size)")
-    return out
-
-
-C_SOLID = float(np.sqrt(3.5 * (5e6 + 3.2e10) / 2700.0))
-
-
-def _wall_solver_kwargs(p):
-    return dict(model=5, order=2, rk_steps=2, gamma=p["gamma"], pinf=p["pinf"], mu=p["mu"],
-                amin=p["amin"], avf_lim=p["avf_lim"], prelax=3)
+def _config3(name: str):
+    """Bubble collapse near a hyperelastic wall, 3 materials (NEQ 21)."""
+    from forestfv_public_gb300 import workloads as W
+    lmax, band = WALL_SIZES[name]
+    mesh, S0, p = W.bubble_wall_config3(lmax=lmax, band_cells=band)
+    cfg = workload_config(name, int(mesh.n), sorted(int(x) for x in np.unique(mesh.level)))
+    cfg["amr"] = {"tags": list(wall_tags(lmax)), "every": AMR_EVERY, "horizon": AMR_HORIZON,
+                  "threshold": AMR_THRESHOLD, "infer_every": AMR_INFER_EVERY}
+    return mesh, S0, cfg["dt"], cfg, _wall_solver_kwargs(p), m5_alg_bytes(21, 3), False
 
 
 def wl_config3(small: bool = False, medium: bool = False):
-    """Bubble collapse near a hyperelastic wall, 3 materials (NEQ 21), levels 4-9."""
-    from forestfv_public_gb300 import workloads as W
-    if small:  # CPU sample: same physics, levels 4..5
-        lmax, band = 5, 2.0
-    elif medium:  # profiler captures: levels 4..7, 0.41 M cells
-        lmax, band = 7, 4.0
-    else:
-        lmax, band = 9, 6.5
-    mesh, S0, p = W.bubble_wall_config3(lmax=lmax, band_cells=band)
-    hmin = 0.5 / (1 << (lmax - 1))
-    dt = 0.01 * hmin / C_SOLID
-    neq = S0.shape[0]
-    size = f"levels 4-{lmax}"
-    state_mb = 8 * neq * mesh.n / 1e6
-    cfg = {"workload": f"config3 bubble collapse near a hyperelastic wall, model 5 (3 materials), "
-                       f"{size} AMR, plain FP64, MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
-           "cells": int(mesh.n), "levels": sorted(int(x) for x in np.unique(mesh.level)),
-           "neq": neq, "dt": float(dt), "cfl": 0.01, "cfl_speed": "solid sound speed, finest cell",
-           "parallelism": "single GPU",
-           "l2": f"state {state_mb:.0f} MB > L2 (129 MB): no flush needed"}
-    cfg["amr"] = {"tags": list(wall_tags(lmax)), "every": AMR_EVERY, "horizon": AMR_HORIZON,
-                  "threshold": AMR_THRESHOLD, "infer_every": AMR_INFER_EVERY}
-    return mesh, S0, dt, cfg, _wall_solver_kwargs(p), m5_alg_bytes(neq, 3), False
+    return _config3("config3s" if small else "config3m" if medium else "config3")
 
 
-AMR_EVERY, AMR_HORIZON, AMR_THRESHOLD = 8, 16, 0.3
+def wl_config3m(small: bool = False):
+    """config3 physics on a 0.41 M-cell mesh (levels 4-7): the size profiler captures use."""
+    return _config3("config3s" if small else "config3m")
+
+
+AMR_EVERY, AMR_HORIZON, AMR_THRESHOLD = 8, 8, 0.3
 # the network runs every step, as the learned-indicator configuration specifies (AdaptiveRun
 # takes infer_every > 1 too: a mark predicts a refinement within AMR_HORIZON steps and the
 # marks accumulate until the next regrid)
@@ -191,11 +205,6 @@ def m5_alg_bytes(neq: int, nmat: int) -> dict:
             "m5f_face_flux": 6 * rec + 8 * 2 * nmat + 28 + 6 * 4 * neq + 6 * 3 * 4 + 6 * 8,
             "m5f_cell_update": d + 6 * 4 * neq + 6 * 3 * 4 + d + 28 + d + d + 1,
             "m5f_relax_cell": d + d + 1}
-
-
-def wl_config3m(small: bool = False):
-    """config3 physics on a 0.41 M-cell mesh (levels 4-7): the size profiler captures use."""
-    return wl_config3(small=small, medium=not small)
 
 
 WORKLOADS = {"config2": wl_config2, "config1": wl_config1, "config2m": wl_config2m,
@@ -290,72 +299,131 @@ def ncu_summary(kernel: str, cells: int, workload: str):
     return None, None
 
 
-_CPU_CACHE = {}
+# ------------------------------------------------------------------------ CPU legs
+# The reference algorithm on the host cores: the oracle's C restatement (oracle/, the
+# reference's m0/m5 step function by function) on contiguous Morton ranges of the stated
+# workload's own mesh.  The mesh is generated and its reference-form geometry built in numpy
+# (oracle/forest.py), so these legs map no library of the product.  A range is advanced as a
+# mesh of its own (faces to cells outside it transmissive); every cell of it is a full
+# cell-update of the workload's physics at its own level.
 
 
-def cpu_sample(workload: str, seconds: float = 10.0):
-    """Time the oracle's C restatement on the workload's CPU sample, one core."""
+def cpu_case(workload: str):
+    """(forest, initial-state function, dt, solver keywords, mesh description) of a
+    workload, built in numpy only."""
+    from forestfv_public_gb300 import workloads as W
+    from oracle.forest import Forest
+    if workload == "config1":
+        from forestfv_public_gb300.mesh import uniform_leaves
+        lv = uniform_leaves((4, 4, 4), 4)
+        F = Forest((4, 4, 4), lv.tree_ijk, lv.level, lv.cell_ijk)
+        return F, sod_state, 0.4 * (1.0 / 32.0) / np.sqrt(1.4), dict(model=0), "32^3 uniform"
+    if workload.startswith("config3"):
+        lmax, band = WALL_SIZES[workload]
+        lv, state = W.bubble_wall_parts(lmax=lmax, band_cells=band)
+        kw = _wall_solver_kwargs(W.WALL)
+        dt = 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID
+    else:
+        lmin, lmax, band = BUBBLE_SIZES[workload]
+        lv, state = W.bubble_config2_parts(lmin=lmin, lmax=lmax, band_cells=band)
+        kw = _bubble_solver_kwargs(W.BUBBLE)
+        dt = 0.01 * (0.5 / (1 << (lmax - 1))) / C_LIQUID
+    F = Forest((2, 2, 2), lv.tree_ijk, lv.level, lv.cell_ijk)
+    return F, state, dt, kw, f"levels {int(lv.level.min())}-{lmax}, {F.n} cells as generated"
+
+
+def _cpu_advance(om, S_aos, dt, steps, kw, flux_form):
     from oracle import pyoracle
-    if workload not in _CPU_CACHE:
-        mesh, S0, dt, _, kw, _, _ = WORKLOADS[workload](small=True)
-        _CPU_CACHE[workload] = (mesh, S0, dt, kw, pyoracle.OracleMesh(mesh.export()))
-    mesh, S0, dt, kw, om = _CPU_CACHE[workload]
-    S = np.ascontiguousarray(S0.T)
+    if kw.get("model", 0) == 5:
+        m5 = dict(avf_lim=kw["avf_lim"], prelax=kw["prelax"], amin=kw["amin"],
+                  pinf=list(kw["pinf"]), gamma=list(kw["gamma"]), mu=list(kw["mu"]),
+                  flux_form=flux_form)
+        return pyoracle.m5_advance(om, S_aos, dt, steps, m5)
+    return pyoracle.m0_advance(om, S_aos, dt, steps)
 
-    def adv(S, k):
-        if kw.get("model", 0) == 5:
-            m5 = dict(avf_lim=kw["avf_lim"], prelax=kw["prelax"], amin=kw["amin"],
-                      pinf=list(kw["pinf"]), gamma=list(kw["gamma"]), mu=list(kw["mu"]))
-            return pyoracle.m5_advance(om, S, dt, k, m5)
-        return pyoracle.m0_advance(om, S, dt, k)
 
+def _cpu_range_worker(job):
+    """One worker's share of a round: one untimed step of its range, then `steps` timed
+    steps.  Returns (cells, steps, seconds)."""
+    from oracle import pyoracle
+    geo, S, dt, kw, flux_form, steps = job
+    om = pyoracle.OracleMesh(geo)
+    S = _cpu_advance(om, np.ascontiguousarray(S.T), dt, 1, kw, flux_form)
     t0 = time.perf_counter()
-    S = adv(S, 1)
-    one = time.perf_counter() - t0
-    steps = max(1, min(200, int(seconds / max(one, 1e-6))))
-    t0 = time.perf_counter()
-    adv(S, steps)
-    el = time.perf_counter() - t0
-    return mesh.n * steps / el, steps, mesh.n
+    _cpu_advance(om, S, dt, steps, kw, flux_form)
+    return om.n, steps, time.perf_counter() - t0
 
 
-def _cpu_worker(args):
-    workload, seconds = args
-    return cpu_sample(workload, seconds)
+class CpuSampler:
+    """The reference algorithm timed on `cores` host processes over contiguous Morton ranges
+    of a workload's mesh.  Each round gives every worker its own range (the ranges of all
+    rounds spread evenly over the mesh); a worker times only its steady steps, and a round's
+    rate is the sum of its workers' rates (they run at once, one per core)."""
+
+    def __init__(self, workload: str, cores: int, flux_form: int, seconds: float = 1.0):
+        from multiprocessing import get_context
+        self.F, self.state, self.dt, self.kw, self.mesh_desc = cpu_case(workload)
+        self.cores, self.flux_form = cores, flux_form
+        self.pool = get_context("spawn").Pool(cores)
+        # range size from a probe step: about `seconds` of steady work per worker and round
+        probe = min(self.F.n, 4096)
+        n, k, el = _cpu_range_worker(self._job(0, probe, 1))
+        self.R = int(min(self.F.n, max(2048, seconds * n * k / max(el, 1e-9))))
+
+    def _job(self, start, R, steps):
+        sel = np.arange(start, start + R)
+        return (self.F.geometry(sel), self.state(self.F.centroids(sel)), self.dt, self.kw,
+                self.flux_form, steps)
+
+    def round(self, index: int, rounds: int, steps: int = 1):
+        """Returns (summed rate in cell-updates/s, the slowest worker's seconds)."""
+        jobs = []
+        for w in range(self.cores):
+            i = index * self.cores + w
+            c = int((i + 0.5) * self.F.n / (rounds * self.cores)) - self.R // 2
+            jobs.append(self._job(min(max(c, 0), self.F.n - self.R), self.R, steps))
+        res = self.pool.map(_cpu_range_worker, jobs)
+        return sum(n * k / el for n, k, el in res), max(el for _, _, el in res)
+
+    def describe(self, rounds: int, steps: int = 1) -> str:
+        return (f"{self.cores} processes x {rounds} rounds; each process advances a contiguous "
+                f"Morton range of {self.R} cells of the workload's mesh ({self.mesh_desc}) "
+                f"by one untimed and {steps} timed time step(s) of the oracle's C restatement "
+                "of the reference algorithm; ranges spread evenly over the mesh, faces leaving "
+                "a range transmissive; rate = sum of the processes' rates")
+
+    def close(self):
+        self.pool.close()
+        self.pool.join()
 
 
-# ------------------------------------------------------------------------------ arms
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from multiprocessing import get_context
-    from oracle import pyoracle
-    pyoracle.lib()  # build once before the workers start
     cores = os.cpu_count() or 1
-    full_cfg = WORKLOADS[args.workload]()[3]
-    per_step = []
-    ctx = get_context("spawn")
-    per_step_s = max(0.5, min(3.0, 120.0 / max(1, args.steps)))
-    with ctx.Pool(cores) as pool:
-        for _ in range(args.warmup):
-            pool.map(_cpu_worker, [(args.workload, 0.2)] * cores)
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            res = pool.map(_cpu_worker, [(args.workload, per_step_s)] * cores)
-            el = time.perf_counter() - t0
-            per_step.append(sum(r[1] * r[2] for r in res) / el)
-    value = statistics.median(per_step)
-    steps, n = res[0][1], res[0][2]
+    flux_form = FLUX_FORMS[args.flux_form]
+    cfg = workload_config(args.workload)
+    sampler = CpuSampler(args.workload, cores, flux_form)
+    for r in range(args.warmup):
+        sampler.round(r, args.warmup)
+    rates, secs = [], []
+    for r in range(args.steps):
+        rate, el = sampler.round(r, args.steps)
+        rates.append(rate)
+        secs.append(el)
+    sampler.close()
+    value = statistics.median(rates)
+    cfg["sample"] = {"cells_per_round": sampler.R * cores, "range_cells": sampler.R,
+                     "processes": cores, "mesh": sampler.mesh_desc,
+                     "fraction_of_mesh_per_round": sampler.R * cores / sampler.F.n}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "dtype": "f64", "data": "synthetic", "config": full_cfg, "vs_baseline": None,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(secs),
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic", "config": cfg,
+        "vs_baseline": None,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} processes x {steps} steps of a {n}-cell mesh of the "
-                                   "same problem (oracle C restatement of the reference "
-                                   "algorithm; the reference's own binary is not built on "
-                                   "this host)"},
+                         "sample": sampler.describe(args.steps)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -424,13 +492,72 @@ def measure_fp32_form(mesh, S0, dt, kw, args, dev, fp64_solver) -> dict:
     s32.close()
     return {"value": mesh.n * args.steps / (t_ms / 1e3), "unit": UNIT,
             "ms_per_step": t_ms / args.steps, "kernel_mean_ms_per_stage": mean_ms,
+            "flux_form": FLUX_FORM_NOTE[kw.get("flux_form", 0)],
             "error_vs_fp64": err, "error_steps": args.steps,
+            "gate": accuracy_gate(err, args.steps, kw.get("mu")),
             "fp64_sensitivity_floor": {"perturbation": FP32_PERTURBATION, **floor},
             "error_growth": growth,
-            "note": "error of the FP32-flux form against the FP64 form after error_steps steps, "
-                    "beside the FP64 form's own change when its initial state is perturbed by "
-                    "1e-7 relative: the reference's model-5 scheme amplifies rounding-level "
-                    "differences, so the FP32 form is judged against that floor"}
+            "note": "error of the FP32-flux form against the FP64 form on the same mesh after "
+                    "error_steps steps, beside the FP64 form's own change when its initial state "
+                    "is perturbed by 1e-7 relative (the sensitivity of the scheme itself)"}
+
+
+GATE_BAR = 1e-4
+# the smallest wall stress whose relative error the gate takes as it is: a strain of 1e-6
+# (stress 1e-6 mu, ~16 FP32 ulps of the deformation tensor); below it the peak is rounding
+# noise of a solid not yet loaded, and its error is taken relative to this scale
+WALL_STRAIN_SCALE = 1e-6
+
+
+def accuracy_gate(err: dict, steps: int, mu=None) -> dict:
+    """The metric's accuracy condition on an error report: relative L1 error of density and
+    the error of the peak wall stress, each <= 1e-4.  The wall stress error is relative to
+    the larger of the FP64 peak and 1e-6 of the solid's shear modulus; the plain relative
+    error is reported beside it."""
+    rho = err["rho"]["rel_l1"]
+    out = {"bar": GATE_BAR, "steps": steps, "rho_rel_l1": rho}
+    ok = rho <= GATE_BAR
+    w = err.get("peak_wall_stress")
+    if w is not None:
+        scale = max(abs(w["ref"]), WALL_STRAIN_SCALE * max(mu or (0.0,)))
+        rel = abs(w["test"] - w["ref"]) / max(scale, 1e-300)
+        out.update({"peak_wall_stress_fp64": w["ref"], "peak_wall_stress_test": w["test"],
+                    "peak_wall_stress_rel_err": w["rel_err"],
+                    "peak_wall_stress_err_of_scale": rel, "wall_stress_scale": scale})
+        ok = ok and rel <= GATE_BAR
+    out["pass"] = bool(ok)
+    return out
+
+
+def gate_medium(kw: dict, dev, counts=(20, 100)) -> dict:
+    """The accuracy condition on the medium wall mesh (0.41 M cells, levels 4-7), where the
+    wall is loaded within the first steps (peak wall stress 3e5 Pa after 20 steps): the
+    FP32-flux form against the FP64 form, same mesh, same flux form."""
+    from forestfv_public_gb300 import Solver
+    from forestfv_public_gb300.fields import error_report
+    mesh, S0, dt, _, kw_m, _, _ = wl_config3m()
+    kw_m = dict(kw_m, flux_form=kw.get("flux_form", 0))
+    a = Solver(device=dev.index, precision=0, **kw_m)
+    b = Solver(device=dev.index, precision=1, **kw_m)
+    for s in (a, b):
+        s.set_mesh(mesh)
+        s.upload_state(S0)
+    out, done = [], 0
+    try:
+        for c in counts:
+            a.step(dt, c - done)
+            b.step(dt, c - done)
+            done = c
+            e = error_report(b.download_state(), a.download_state(), kw_m["gamma"], kw_m["pinf"],
+                             kw_m["mu"], kw_m["amin"], 0)
+            out.append(accuracy_gate(e, c, kw_m["mu"]))
+    except Exception as ex:  # the reference's flux goes non-finite within ~100 steps here
+        out.append({"steps": c, "error": str(ex), "pass": False})
+    finally:
+        a.close()
+        b.close()
+    return {"workload": f"config3m ({mesh.n} cells, levels 4-7)", "gates": out,
+            "pass": all(g["pass"] for g in out)}
 
 
 def train_wall_indicator(kw: dict, dev, amr_cfg: dict, seed: int = 20261203):
@@ -540,6 +667,10 @@ def run_ours(args) -> None:
     torch.cuda.set_device(dev)
 
     mesh, S0, dt, cfg, kw, alg_bytes, flush_l2 = WORKLOADS[args.workload]()
+    flux_form = FLUX_FORMS[args.flux_form]
+    if kw.get("model", 0) == 5:
+        kw["flux_form"] = flux_form
+        cfg["flux_form"] = FLUX_FORM_NOTE[flux_form]
     amr_cfg = cfg.get("amr") if not args.no_amr else None
     solver = Solver(device=local, **kw)
     solver.set_mesh(mesh)
@@ -555,6 +686,8 @@ def run_ours(args) -> None:
         cfg["initial_adaptation"] = {"rounds": rounds, "seconds": time.perf_counter() - t0,
                                      "cells": int(mesh.n),
                                      "levels": sorted(int(x) for x in np.unique(mesh.level))}
+        # the timed loops run on the adapted mesh
+        cfg["cells_generated"], cfg["cells"] = cfg["cells"], int(mesh.n)
     neq = solver.neq
     stream = torch.cuda.ExternalStream(solver.stream_handle(), device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev) if flush_l2 else None
@@ -629,11 +762,13 @@ def run_ours(args) -> None:
 
     if rank == 0:
         cpu = None
-        if world == 1:
-            rate, csteps, n = cpu_sample(args.workload, args.cpu_seconds)
-            cpu = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-                   "sample": f"{csteps} steps of a {n}-cell mesh of the same problem, oracle C "
-                             "restatement of the reference algorithm"}
+        if world == 1 and args.cpu_rounds > 0:
+            cores = os.cpu_count() or 1
+            sampler = CpuSampler(args.workload, cores, flux_form)
+            rates = [sampler.round(r, args.cpu_rounds)[0] for r in range(args.cpu_rounds)]
+            sampler.close()
+            cpu = {"value": statistics.median(rates), "unit": UNIT, "cores": cores, "kind": "port",
+                   "sample": sampler.describe(args.cpu_rounds)}
         fp32 = None
         if world == 1 and kw.get("model", 0) == 5 and not args.no_fp32_form:
             fp32 = measure_fp32_form(mesh, S0, dt, kw, args, dev, solver)
@@ -654,6 +789,35 @@ def run_ours(args) -> None:
             line["plain_fp64_form"] = fp64_line
         if fp32 is not None:
             line["fp32_flux_form"] = fp32
+        if "learned_amr" in line and fp32 is not None:
+            # the metric's accuracy condition at the timed step count: the FP32-flux form
+            # against the FP64 form on the same mesh, and the headline run (FP32 flux +
+            # learned AMR) against the comparator (FP64 + the reference's AMR)
+            g_same, g_run = fp32["gate"], line["learned_amr"]["gate"]
+            g_med = gate_medium(kw, dev) if args.workload == "config3" else None
+            line["accuracy_gate"] = {"bar": GATE_BAR, "steps": args.steps,
+                                     "fp32_vs_fp64_same_mesh": g_same,
+                                     "learned_amr_vs_plain_fp64_amr": g_run,
+                                     "medium_mesh_loaded_wall": g_med,
+                                     "pass": bool(g_same["pass"] and g_run["pass"]
+                                                  and (g_med is None or g_med["pass"])),
+                                     "flux_form": FLUX_FORM_NOTE[flux_form],
+                                     "wall_stress_note":
+                                         "wall stress error relative to max(FP64 peak, 1e-6 of "
+                                         "the solid's shear modulus); the plain relative error "
+                                         "is beside it"}
+        if (world == 1 and kw.get("model", 0) == 5 and flux_form != 0 and not args.no_fp32_form
+                and not args.no_reference_form):
+            # the same FP32-flux error report with the reference's own m5 flux
+            kref = dict(kw, flux_form=0)
+            s64 = Solver(device=local, **kref)
+            s64.set_mesh(mesh)
+            s64.upload_state(S0)
+            rf = measure_fp32_form(mesh, S0, dt, kref, args, dev, s64)
+            s64.close()
+            line["reference_flux_form"] = {k: rf[k] for k in (
+                "value", "ms_per_step", "flux_form", "error_vs_fp64", "gate",
+                "fp64_sensitivity_floor", "error_growth")}
         line["clocks"] = clocks.stop()
         print(json.dumps(line), flush=True)
     else:
@@ -730,6 +894,7 @@ def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, ke
                         "every": every, "horizon": amr_cfg["horizon"], "threshold": thr,
                         "infer_every": amr_cfg.get("infer_every", 1),
                         "error_vs_plain_fp64_amr": err,
+                        "gate": accuracy_gate(err, args.steps, mu),
                         "speedup_vs_plain_fp64_amr": value / plain_value},
     }
     for s in (sp, sl, se):
@@ -745,7 +910,14 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--workload", default="config3", choices=tuple(WORKLOADS))
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-rounds", type=int, default=3,
+                    help="rounds of the CPU baseline (all host cores, one range each); 0 skips it")
+    ap.add_argument("--flux-form", default="consistent", choices=tuple(FLUX_FORMS),
+                    help="model 5's flux: the reference's as written, or made consistent "
+                         "(include/ffv.h FFV_FLUX_CONSISTENT); the default is the one whose "
+                         "FP32-flux form meets the metric's accuracy condition")
+    ap.add_argument("--no-reference-form", action="store_true",
+                    help="skip the FP32-flux error report with the reference's own flux")
     ap.add_argument("--no-amr", action="store_true",
                     help="skip the time loops with mesh adaptation (headline = plain FP64)")
     ap.add_argument("--no-fp32-form", action="store_true",

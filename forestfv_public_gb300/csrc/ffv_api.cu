@@ -119,9 +119,11 @@ int alloc_mesh_buffers(ffv_ctx *c) {
   return FFV_OK;
 }
 
+// a non-positive density is reported before the NaN it leads to (a negative density gives a
+// NaN sound speed within the same stage)
 unsigned status_to_err(unsigned st) {
-  if (st & (FFV_ST_NAN | FFV_ST_NAN_SPEED | FFV_ST_NO_BRANCH)) return FFV_ERR_NAN;
   if (st & FFV_ST_NEG_DENSITY) return FFV_ERR_NEG_DENSITY;
+  if (st & (FFV_ST_NAN | FFV_ST_NAN_SPEED | FFV_ST_NO_BRANCH)) return FFV_ERR_NAN;
   return FFV_OK;
 }
 

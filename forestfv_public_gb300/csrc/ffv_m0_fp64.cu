@@ -221,7 +221,9 @@ __global__ void __launch_bounds__(128) m0_flux_rk(ffv_dmesh m, ffv_geom g,
   const uint32_t info = m.info[c];
   const int l = ffv_info_level(info);
   double rhs[NV] = {0.0, 0.0, 0.0, 0.0, 0.0};
-  unsigned st = 0;
+  // a non-positive density in the stage's input (the reference runs on into a NaN sound
+  // speed there); the status word reports it, the arithmetic is untouched
+  unsigned st = S[c] <= 0.0 ? FFV_ST_NEG_DENSITY : 0u;
   st |= face_residual<ORDER, 0>(m, g, FS, c, info, l, gamma, pinf, rhs);
   st |= face_residual<ORDER, 1>(m, g, FS, c, info, l, gamma, pinf, rhs);
   st |= face_residual<ORDER, 2>(m, g, FS, c, info, l, gamma, pinf, rhs);
@@ -251,6 +253,7 @@ __global__ void __launch_bounds__(128) m0_flux_rk(ffv_dmesh m, ffv_geom g,
         out = (1.0 / 2.0) * sn + (1.0 / 2.0) * s - (1.0 / 2.0) * dt * rhs[e] / V;
     }
     S[k] = out;
+    if (e == 0 && out <= 0.0) st |= FFV_ST_NEG_DENSITY;
   }
   if (st) atomicOr(status, st);
 }

@@ -211,12 +211,16 @@ struct NCf {
   float unc[3], avf[N], are[N], A[9];
 };
 
-// m5_star_region.c:3-158 in FP32
+// m5_star_region.c:3-158 in FP32.  dU receives the jump U*_K - U_K of the conservative
+// variables (what the HLLC correction S_K (U*_K - U_K) needs).  With the consistent flux
+// form the jumps of the partial densities and of the total energy are formed as differences,
+// never as U*_K minus U_K: the solid's total energy is ~5e10 J/m^3 (p_inf 3.2e10), whose FP32
+// ulp (4096) would otherwise enter every face's energy flux as noise even at rest.
 template <int F, int N>
 __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const SolF<N> &L,
                                   const SolF<N> &R, bool leftside, float u_S, float SL, float SR,
                                   float uL, float vL, float wL, float uR, float vR, float wR,
-                                  const float sL[3], const float sR[3], float *Us, NCf<N> &nc) {
+                                  const float sL[3], const float sR[3], float *dU, NCf<N> &nc) {
   using C = K5<N>;
   float SK, uK, vK, wK, s11K, s12K, s13K;
   if (leftside) {
@@ -286,11 +290,19 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
     const float e_S = (p_S + ga * pi) / (rm_S * (ga + 1.0f)) + eel;
     nc.are[v] = ar_S[v] * e_S;
   }
+  if (k.flux_form == FFV_FLUX_CONSISTENT) {
+    const float iw = 1.0f / (SK - u_S);
 #pragma unroll
-  for (int v = 0; v < N; ++v) Us[C::i0 + v] = ar_S[v];
+    for (int v = 0; v < N; ++v) dU[C::i0 + v] = s.ra[v] * (u_S - uK) * iw;
+    dU[C::i2] = (re * (uK - u_S) - s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
+                 s13_S * w_S) / (u_S - SK);
+  } else {
 #pragma unroll
-  for (int v = 0; v < 3; ++v) Us[C::i1 + v] = r_S * vel[v];
-  Us[C::i2] = r_S * Em_S;
+    for (int v = 0; v < N; ++v) dU[C::i0 + v] = ar_S[v] - s.vec[C::i0 + v];
+    dU[C::i2] = r_S * Em_S - s.vec[C::i2];
+  }
+#pragma unroll
+  for (int v = 0; v < 3; ++v) dU[C::i1 + v] = r_S * vel[v] - s.vec[C::i1 + v];
 #pragma unroll
   for (int d = 0; d < 3; d++) nc.unc[d] = vel[d];
 #pragma unroll
@@ -302,7 +314,7 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
   unsigned st = 0;
 #pragma unroll
   for (int iv = 0; iv < C::NC; ++iv)
-    if (isnan(Us[iv])) st |= FFV_ST_NAN;
+    if (isnan(dU[iv])) st |= FFV_ST_NAN;
   return st;
 }
 
@@ -382,7 +394,7 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
   unsigned st = (isnan(u_S) || isnan(SR) || isnan(SL)) ? FFV_ST_NAN_SPEED : 0u;
   if (!gfm && bc == 4) u_S = 0.0f;
   NCf<N> nc;
-  float Fn[C::NEQ], Us[C::NC], corr[C::NC];
+  float Fn[C::NEQ], dU[C::NC], corr[C::NC];
 #pragma unroll
   for (int iv = 0; iv < C::NC; ++iv) corr[iv] = 0.0f;
   const bool left_star = gfm ? (SL < 0.0f && 0.0f <= u_S) : (SL <= 0.0f && 0.0f <= u_S);
@@ -390,15 +402,15 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
   if (0.0f <= SL) {
     flux_n_f<F>(L, 0, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
   } else if (left_star) {
-    st |= star_region_f<F>(k, L, L, R, true, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
+    st |= star_region_f<F>(k, L, L, R, true, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, dU, nc);
     flux_n_f<F>(L, 1, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
 #pragma unroll
-    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SL * (Us[iv] - L.vec[iv]);
+    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SL * dU[iv];
   } else if (right_star) {
-    st |= star_region_f<F>(k, R, L, R, false, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, Us, nc);
+    st |= star_region_f<F>(k, R, L, R, false, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, dU, nc);
     flux_n_f<F>(R, 2, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
 #pragma unroll
-    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SR * (Us[iv] - R.vec[iv]);
+    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SR * dU[iv];
   } else if (SR <= 0.0f) {
     flux_n_f<F>(R, 3, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
   } else {
@@ -1245,7 +1257,11 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
   for (int iv = 0; iv < N; iv++) r[C::i4 + iv] += (double)nc[N - 1 + iv];
 #pragma unroll
   for (int q = 0; q < 9; q++) r[C::i5 + q] = (double)(rhsA[q] + nc[2 * N - 1 + q]);
-  unsigned st = 0;
+  // a non-positive density in the stage's input is reported (the arithmetic is untouched)
+  double rho_in = 0.0;
+#pragma unroll
+  for (int v = 0; v < N; ++v) rho_in += s[C::i0 + v];
+  unsigned st = rho_in <= 0.0 ? FFV_ST_NEG_DENSITY : 0u;
 #pragma unroll
   for (int iv = 0; iv < C::NEQ; iv++) {
     if (isnan(r[iv])) st |= FFV_ST_NAN;

@@ -989,7 +989,11 @@ __global__ void __launch_bounds__(128) m5_cell_update(ffv_dmesh m, ffv_geom g, M
   }
   FACE(0) FACE(1) FACE(2) FACE(3) FACE(4) FACE(5)
 #undef FACE
-  unsigned st = 0;
+  // a non-positive density in the stage's input is reported (the arithmetic is untouched)
+  double rho_in = 0.0;
+#pragma unroll
+  for (int v = 0; v < N; ++v) rho_in += s[C::i0 + v];
+  unsigned st = rho_in <= 0.0 ? FFV_ST_NEG_DENSITY : 0u;
 #pragma unroll
   for (int iv = 0; iv < C::NEQ; iv++) {
     if (isnan(rhs[iv])) st |= FFV_ST_NAN;

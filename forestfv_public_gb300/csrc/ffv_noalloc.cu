@@ -180,7 +180,7 @@ extern "C" int ffv_step_noalloc(const ffv_mesh *m, const ffv_params *p, double *
           cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return FFV_ERR_CUDA;
-  if (h_status & (FFV_ST_NAN | FFV_ST_NAN_SPEED | FFV_ST_NO_BRANCH)) return FFV_ERR_NAN;
   if (h_status & FFV_ST_NEG_DENSITY) return FFV_ERR_NEG_DENSITY;
+  if (h_status & (FFV_ST_NAN | FFV_ST_NAN_SPEED | FFV_ST_NO_BRANCH)) return FFV_ERR_NAN;
   return FFV_OK;
 }

@@ -147,17 +147,36 @@ def test_gpu_conservation_reflective_box(built_lib):
         assert abs(tot1 - tot0) <= 1e-12 * abs(tot0) * 10, (v, tot0, tot1)
 
 
-def test_nan_state_is_reported(built_lib):
+def test_negative_density_is_reported(built_lib):
+    """A negative density injected on the host into the uploaded state: the device status
+    word reports FFV_ERR_NEG_DENSITY (the reference would run on into a NaN sound speed)."""
     g = load_golden("m0_sod_uniform")
     m = mesh_from_golden(g)
     S = g["S_init"].copy()
-    S[17, 0] = -1.0  # negative density -> NaN sound speed
+    S[17, 0] = -1.0
+    s = Solver()
+    s.set_mesh(m)
+    s.upload_state(S.T.copy())
+    with pytest.raises(FFVError) as e:
+        s.step(1e-3, 1)
+    assert e.value.code == 6
+    s.close()
+
+
+def test_nan_state_is_reported(built_lib):
+    """A NaN injected on the host into the uploaded state: FFV_ERR_NAN from the status word
+    (m0_residual.c:127-135 exits there)."""
+    g = load_golden("m0_sod_uniform")
+    m = mesh_from_golden(g)
+    S = g["S_init"].copy()
+    S[17, 4] = np.nan
     s = Solver()
     s.set_mesh(m)
     s.upload_state(S.T.copy())
     with pytest.raises(FFVError) as e:
         s.step(1e-3, 1)
     assert e.value.code == 5
+    s.close()
 
 
 def test_cfl_dt(built_lib):

@@ -79,6 +79,26 @@ def test_m5_nan_wave_speed_reported(built_lib):
     assert e.value.code == 5
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_m5_negative_density_reported(precision, built_lib):
+    """A negative partial density injected on the host (both forms): FFV_ERR_NEG_DENSITY."""
+    from forestfv_public_gb300 import FFVError
+    g = load_golden("m5_wall_amr")
+    m = mesh_from_golden(g)
+    q = m5_params(g)
+    s = Solver(model=5, order=int(g["order"]), rk_steps=int(g["rk_steps"]), gamma=q["gamma"],
+               pinf=q["pinf"], mu=q["mu"], amin=q["amin"], avf_lim=q["avf_lim"],
+               prelax=q["prelax"], precision=precision)
+    s.set_mesh(m)
+    S = np.ascontiguousarray(g["S_init"].T).copy()
+    S[:3, 40] = -S[:3, 40]
+    s.upload_state(S)
+    with pytest.raises(FFVError) as e:
+        s.step(float(g["dt"]), 1)
+    assert e.value.code == 6
+    s.close()
+
+
 def test_cfl_dt_model5(built_lib):
     """ffv_cfl_dt (warp-shuffle min-reduction) against the host restatement:
     dt = cfl * min over cells of h / (max_a |u_a| + c), c^2 = sum_k alpha_k gamma_k
