@@ -81,8 +81,11 @@ def _bubble_solver_kwargs(p):
 
 
 def _wall_solver_kwargs(p):
+    """The wall configurations' solver: the solid elastoplastic with its von Mises yield
+    stress (a J2 radial return after each relaxation; the reference's solid is hyperelastic)."""
     return dict(model=5, order=2, rk_steps=2, gamma=p["gamma"], pinf=p["pinf"], mu=p["mu"],
-                amin=p["amin"], avf_lim=p["avf_lim"], prelax=3)
+                amin=p["amin"], avf_lim=p["avf_lim"], prelax=3,
+                yield_stress=p.get("yield_stress"))
 
 
 C_SOLID = float(np.sqrt(3.5 * (5e6 + 3.2e10) / 2700.0))
@@ -90,6 +93,8 @@ C_SOLID = float(np.sqrt(3.5 * (5e6 + 3.2e10) / 2700.0))
 WALL_SIZES = {"config3": (9, 6.5), "config3m": (7, 4.0), "config3s": (5, 2.0)}
 # (lmin, lmax, band)
 BUBBLE_SIZES = {"config2": (4, 8, 22.0), "config2m": (4, 7, 12.0), "config2s": (4, 6, 2.0)}
+# 64-bubble stress test: (base level, finest level)
+FIELD_SIZES = {"config5": (8, 10), "config5m": (6, 8), "config5s": (4, 6)}
 FLUX_FORMS = {"reference": 0, "consistent": 1}
 FLUX_FORM_NOTE = {
     0: "the reference's m5 flux as written (m5_star_region.c:59, m5_flux.c:20-34, 53-56)",
@@ -114,6 +119,18 @@ def workload_config(workload: str, n: int | None = None, levels=None) -> dict:
         return {"workload": f"config3 bubble collapse near a hyperelastic wall{size}, model 5 "
                             f"(3 materials), levels 4-{lmax} AMR; FP32-flux + learned AMR against "
                             "plain FP64 + AMR; MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
+                "cells": n, "levels": levels, "neq": 21,
+                "dt": 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": 0.01,
+                "cfl_speed": "solid sound speed, finest cell", "parallelism": "single GPU",
+                "l2": f"state {8 * 21 * n / 1e6:.0f} MB > L2 (129 MB): no flush needed"}
+    if workload.startswith("config5"):
+        lbase, lmax = FIELD_SIZES[workload]
+        size = {"config5": "", "config5m": " (medium size)", "config5s": " (small size)"}[workload]
+        return {"workload": f"config5 throughput stress test{size}: 64 seeded gas bubbles "
+                            f"(radii U(0.02, 0.05), liquid at one seeded pressure U(1, 10) MPa) above "
+                            f"the solid half-space, uniform level {lbase} refined to level {lmax} "
+                            "at the interfaces, model 5 (3 materials); FP32-flux + learned AMR "
+                            "against plain FP64 + AMR; MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
                 "cells": n, "levels": levels, "neq": 21,
                 "dt": 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": 0.01,
                 "cfl_speed": "solid sound speed, finest cell", "parallelism": "single GPU",
@@ -207,8 +224,32 @@ def m5_alg_bytes(neq: int, nmat: int) -> dict:
             "m5f_relax_cell": d + d + 1}
 
 
+def _config5(name: str):
+    """The 64-bubble throughput stress test above the solid half-space, 3 materials."""
+    from forestfv_public_gb300 import workloads as W
+    lbase, lmax = FIELD_SIZES[name]
+    mesh, S0, p = W.bubble_field_config5(lbase=lbase, lmax=lmax)
+    cfg = workload_config(name, int(mesh.n), sorted(int(x) for x in np.unique(mesh.level)))
+    # uniform base level, density jump and four interface layers (the generator's band) to
+    # the finest level
+    cfg["amr"] = {"tags": [1, lbase, 0, 0, 0.0, 1, lmax, 0.1, 0, 0, 0.0, 1, lmax, 4, 0, 0, 0],
+                  "every": AMR_EVERY, "horizon": AMR_HORIZON, "threshold": AMR_THRESHOLD,
+                  "infer_every": AMR_INFER_EVERY}
+    return mesh, S0, cfg["dt"], cfg, _wall_solver_kwargs(p), m5_alg_bytes(21, 3), False
+
+
+def wl_config5(small: bool = False, medium: bool = False):
+    return _config5("config5s" if small else "config5m" if medium else "config5")
+
+
+def wl_config5m(small: bool = False):
+    """config5 physics on a 1.9 M-cell mesh (levels 6-8)."""
+    return _config5("config5s" if small else "config5m")
+
+
 WORKLOADS = {"config2": wl_config2, "config1": wl_config1, "config2m": wl_config2m,
-             "config3": wl_config3, "config3m": wl_config3m}
+             "config3": wl_config3, "config3m": wl_config3m, "config5": wl_config5,
+             "config5m": wl_config5m}
 
 
 # ------------------------------------------------------------------------------ helpers
@@ -323,6 +364,11 @@ def cpu_case(workload: str):
         lv, state = W.bubble_wall_parts(lmax=lmax, band_cells=band)
         kw = _wall_solver_kwargs(W.WALL)
         dt = 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID
+    elif workload.startswith("config5"):
+        lbase, lmax = FIELD_SIZES[workload]
+        lv, state, _, _ = W.bubble_field_parts(lbase=lbase, lmax=lmax)
+        kw = _wall_solver_kwargs(W.WALL)
+        dt = 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID
     else:
         lmin, lmax, band = BUBBLE_SIZES[workload]
         lv, state = W.bubble_config2_parts(lmin=lmin, lmax=lmax, band_cells=band)
@@ -337,7 +383,7 @@ def _cpu_advance(om, S_aos, dt, steps, kw, flux_form):
     if kw.get("model", 0) == 5:
         m5 = dict(avf_lim=kw["avf_lim"], prelax=kw["prelax"], amin=kw["amin"],
                   pinf=list(kw["pinf"]), gamma=list(kw["gamma"]), mu=list(kw["mu"]),
-                  flux_form=flux_form)
+                  flux_form=flux_form, **{"yield": list(kw.get("yield_stress") or ())})
         return pyoracle.m5_advance(om, S_aos, dt, steps, m5)
     return pyoracle.m0_advance(om, S_aos, dt, steps)
 

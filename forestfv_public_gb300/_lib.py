@@ -39,7 +39,8 @@ class Params(ctypes.Structure):
                 ("pinf", ctypes.c_double * FFV_MAX_MATERIALS),
                 ("mu", ctypes.c_double * FFV_MAX_MATERIALS),
                 ("amin", ctypes.c_double), ("avf_lim", ctypes.c_double),
-                ("zerou", ctypes.c_int32 * 3), ("flux_form", ctypes.c_int32)]
+                ("zerou", ctypes.c_int32 * 3), ("flux_form", ctypes.c_int32),
+                ("yield_", ctypes.c_double * FFV_MAX_MATERIALS)]
 
 
 class ForestDesc(ctypes.Structure):

@@ -320,6 +320,8 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
   if (p->precision != FFV_FP64 && p->model != 5) return FFV_ERR_UNSUPPORTED;
   if (p->flux_form != FFV_FLUX_REFERENCE && p->flux_form != FFV_FLUX_CONSISTENT) return FFV_ERR_ARG;
   if (p->flux_form != FFV_FLUX_REFERENCE && p->model != 5) return FFV_ERR_UNSUPPORTED;
+  for (int i = 0; i < FFV_MAX_MATERIALS; i++)
+    if (p->yield[i] < 0.0 || p->yield[i] != p->yield[i]) return FFV_ERR_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0)
     return FFV_ERR_CUDA;
@@ -347,6 +349,11 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
     }
     k.amin = p->amin;
     k.avf_lim = p->avf_lim;
+    k.plastic = 0;
+    for (int i = 0; i < FFV_MAX_MATERIALS; i++) {
+      k.yield[i] = (i < p->nmaterials && p->mu[i] != 0.0 && p->yield[i] > 0.0) ? p->yield[i] : 0.0;
+      if (k.yield[i] > 0.0) k.plastic = 1;
+    }
     for (int i = 0; i < FFV_MAX_MATERIALS; i++) {
       const double gm1 = p->gamma[i] - 1.0;
       k.gpi[i] = p->gamma[i] * p->pinf[i];

@@ -13,6 +13,8 @@ struct M5Consts {
   int zerou[3];
   double gamma[FFV_MAX_MATERIALS], pinf[FFV_MAX_MATERIALS], mu[FFV_MAX_MATERIALS];
   double amin, avf_lim;
+  double yield[FFV_MAX_MATERIALS];  // von Mises yield stress per material, 0 = none
+  int plastic;                      // a solid material has a yield stress
   // per material, for the FP32-flux form: gamma p_inf, 1 / (gamma - 1),
   // gamma p_inf / (gamma - 1), 1 / gamma
   double gpi[FFV_MAX_MATERIALS], ig1[FFV_MAX_MATERIALS], gpg[FFV_MAX_MATERIALS],

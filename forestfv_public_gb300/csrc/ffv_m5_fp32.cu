@@ -31,6 +31,7 @@
 #include "ffv_device.cuh"
 #include "ffv_m5.cuh"
 #include "ffv_m5_frame.cuh"
+#include "ffv_plastic.cuh"
 
 namespace {
 
@@ -1319,6 +1320,7 @@ __global__ void __launch_bounds__(128) m5f_relax_cell(int64_t n, M5Consts k,
   load_state<N>(Sin, n, c, s);
   const double phi_old = s[C::i3] - k.avf_lim;
   const unsigned st = relax_cell_df<N>(k, s);
+  if (k.plastic) plastic_return<N>(k, s);  // as the FP64 form: FP64 return after relaxation
   const double phi_new = (k.mu[0] != 0.0) ? s[C::i3] - k.avf_lim : phi_old;
   flag[c] = (phi_old * phi_new < 0.0) ? 1 : 0;
 #pragma unroll

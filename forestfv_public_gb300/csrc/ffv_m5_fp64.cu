@@ -24,6 +24,7 @@
 #include "ffv_device.cuh"
 #include "ffv_m5.cuh"
 #include "ffv_m5_frame.cuh"
+#include "ffv_plastic.cuh"
 
 namespace {
 
@@ -1063,6 +1064,9 @@ __global__ void __launch_bounds__(128) m5_relax_cell(int64_t n, M5Consts k,
   load_state<N>(Sin, n, c, s);
   const double phi_old = s[C::i3] - k.avf_lim;
   const unsigned st = relaxationvec<N>(k, s);
+  // the plastic return where the reference's prototype would run it (m5_relaxation_solid.c:14),
+  // after the relaxation so that the stored state lies on or inside the yield surface
+  if (k.plastic) plastic_return<N>(k, s);
   // phi_new[0] exists in the reference only for a solid material 0 (else no trigger)
   const double phi_new = (k.mu[0] != 0.0) ? s[C::i3] - k.avf_lim : phi_old;
   flag[c] = (phi_old * phi_new < 0.0) ? 1 : 0;

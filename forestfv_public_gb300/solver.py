@@ -67,13 +67,14 @@ class Solver:
     def __init__(self, model: int = 0, order: int = 2, rk_steps: int = 2, gamma=(1.4,),
                  pinf=(0.0,), precision: int = _lib.FFV_FP64, device: int = 0, mu=None,
                  amin: float = 1e-6, avf_lim: float = 0.5, prelax: int = 3, zerou=(0, 0, 0),
-                 flux_form: int = _lib.FFV_FLUX_REFERENCE):
+                 flux_form: int = _lib.FFV_FLUX_REFERENCE, yield_stress=None):
         """model 0: gamma/pinf of the one material.  model 5: per-material gamma, pinf and
         mu (shear modulus, 0 for fluids), AMIN, AVF_LIM, PRELAX (1 or 3), ZEROU masks, and
         the flux form: FFV_FLUX_REFERENCE (the reference's m5 flux as written) or
         FFV_FLUX_CONSISTENT (its star-state energy, momentum-flux sign and deformation-flux
         sign made consistent with the rest of its HLLC solver; a deviation, see
-        include/ffv.h)."""
+        include/ffv.h); yield_stress: von Mises yield stress per material (0 or None: a
+        hyperelastic solid, as the reference), a J2 radial return after each relaxation."""
         L = _lib.lib()
         p = _lib.Params()
         p.model, p.nmaterials, p.order, p.rk_steps, p.precision = model, len(gamma), order, rk_steps, precision
@@ -87,6 +88,8 @@ class Solver:
         p.amin, p.avf_lim = amin, avf_lim
         p.zerou[:] = tuple(zerou)
         p.flux_form = flux_form
+        for i, y in enumerate(yield_stress or ()):
+            p.yield_[i] = y
         self.params = p
         self.neq = 5 if model == 0 else 3 * len(gamma) + 12
         h = ctypes.c_void_p()

@@ -120,7 +120,8 @@ def mixture_state(mat: dict, a_gas: np.ndarray) -> np.ndarray:
 
 
 WALL = dict(gamma=(3.5, 4.4, 1.4), pinf=(3.2e10, 6e8, 0.0), rho=(2700.0, 1000.0, 1.0),
-            p=(5e6, 5e6, 1e5), mu=(2.6e10, 0.0, 0.0), amin=1e-6, avf_lim=0.5)
+            p=(5e6, 5e6, 1e5), mu=(2.6e10, 0.0, 0.0), amin=1e-6, avf_lim=0.5,
+            yield_stress=(3e8, 0.0, 0.0))
 
 
 def bubble_wall_config3(lmin: int = 4, lmax: int = 9, band_cells: float = 6.5,
@@ -208,3 +209,69 @@ def random_blast_m0(mesh: Mesh, seed: int) -> np.ndarray:
     rng = np.random.default_rng(seed)
     return blast_m0(mesh, rng.uniform(0.3, 0.7, 3), rng.uniform(0.08, 0.2),
                     p_in=0.1 * rng.uniform(20.0, 200.0))
+
+
+def bubble_field_parts(lbase: int = 8, lmax: int = 10, band_cells: float = 2.0, nbubbles: int = 64,
+                       rmin: float = 0.02, rmax: float = 0.05, wall_z: float = 0.2,
+                       seed: int = 20261203):
+    """The throughput stress test (the fifth configuration) without the face tables: a
+    uniform level-lbase base mesh (2^3 trees; level 8 is 256^3 cells) holding `nbubbles`
+    non-overlapping gas bubbles, radii uniform in [rmin, rmax], centres drawn by seeded
+    rejection sampling in the liquid above the solid half-space z < wall_z of the wall
+    configuration (at least one radius of liquid between a bubble and the wall, the domain
+    boundary or another bubble), the liquid at one seeded pressure uniform in 1-10 MPa;
+    refined to lmax within band_cells finest cells of every bubble surface and of the wall
+    plane, one level per two cells of the coarser level away from them (2:1 balanced).
+    Returns (leaves, state function of cell centroids, the bubbles as (centres, radii), the
+    liquid pressure)."""
+    rng = np.random.default_rng(seed)
+    p_liq = float(rng.uniform(1e6, 1e7))
+    centres, radii = [], []
+    tries = 0
+    while len(radii) < nbubbles:
+        tries += 1
+        if tries > 200000:
+            raise RuntimeError("could not place the bubbles")
+        r = rng.uniform(rmin, rmax)
+        c = np.array([rng.uniform(2 * r, 1 - 2 * r), rng.uniform(2 * r, 1 - 2 * r),
+                      rng.uniform(wall_z + 2 * r, 1 - 2 * r)])
+        if all(np.linalg.norm(c - c2) > r + r2 + max(r, r2) for c2, r2 in zip(centres, radii)):
+            centres.append(c)
+            radii.append(r)
+    C = np.array(centres)
+    R = np.array(radii)
+    hmin = 0.5 / (1 << (lmax - 1))
+
+    def surface_distance(x, chunk=1 << 20):
+        d = np.abs(x[:, 2] - wall_z)
+        for a in range(0, len(x), chunk):
+            xa = x[a:a + chunk]
+            db = np.abs(np.linalg.norm(xa[:, None, :] - C[None], axis=2) - R[None]).min(axis=1)
+            d[a:a + chunk] = np.minimum(d[a:a + chunk], db)
+        return d
+
+    def target(cen, h):
+        d = surface_distance(cen) - 0.8660254 * h
+        lev = lmax - np.floor(np.maximum(d, 0.0) / (band_cells * hmin * 2.0)).astype(np.int64)
+        return np.maximum(lev, lbase)
+
+    mat = dict(WALL, p=(5e6, p_liq, 1e5))
+
+    def state(x, chunk=1 << 20):
+        a_gas = np.zeros(len(x))
+        for a in range(0, len(x), chunk):
+            xa = x[a:a + chunk]
+            dist = np.linalg.norm(xa[:, None, :] - C[None], axis=2) - R[None]
+            a_gas[a:a + chunk] = (0.5 * (1.0 - np.tanh(dist / (2.0 * hmin)))).max(axis=1)
+        return wall_state(mat, x[:, 2] < wall_z, a_gas)
+
+    leaves = refine_to_target((2, 2, 2), lbase, lmax, target)
+    return leaves, state, (C, R), p_liq
+
+
+def bubble_field_config5(lbase: int = 8, lmax: int = 10, band_cells: float = 2.0,
+                         seed: int = 20261203):
+    """bubble_field_parts as a mesh and state: returns (Mesh, S [21, n], params)."""
+    leaves, state, _, p_liq = bubble_field_parts(lbase, lmax, band_cells, seed=seed)
+    mesh = Mesh((2, 2, 2), leaves)
+    return mesh, state(mesh.centroids()), dict(WALL, p=(5e6, p_liq, 1e5))

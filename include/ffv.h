@@ -109,6 +109,12 @@ typedef struct ffv_params {
   double avf_lim;       /* model 5: AVF_LIM, solid-fraction level of the ghost-fluid interface */
   int32_t zerou[3];     /* model 5: ZEROU0..2 (freeze a velocity component, m5_RK.c:93-122) */
   int32_t flux_form;    /* model 5: FFV_FLUX_REFERENCE (0, default) or FFV_FLUX_CONSISTENT */
+  double yield[FFV_MAX_MATERIALS]; /* model 5: von Mises yield stress of each solid material,
+                           0 = none (hyperelastic, as the reference).  A solid with a yield
+                           stress gets a J2 radial return of its deformation tensor after every
+                           cell relaxation (no counterpart in the reference: its plastic step
+                           is only prototyped, strdata.h:809, and the call commented out,
+                           m5_relaxation_solid.c:14) */
 } ffv_params;
 
 /* A Cartesian forest: ntrees[0] x ntrees[1] x ntrees[2] cubic hex trees of edge

@@ -65,6 +65,9 @@ typedef struct ffvo_m5_params {
   double gamma[4], pinf[4], mu[4];  /* MATERGAMA, MATERPINF, MATERMUSH */
   double amin;       /* AMIN */
   double avf_lim;    /* AVF_LIM */
+  double yield[4];   /* von Mises yield stress per material, 0 = none (no reference
+                        counterpart: the reference's plastic step is only prototyped,
+                        strdata.h:809, and its call commented out, m5_relaxation_solid.c:14) */
 } ffvo_m5_params;
 
 /* Advance S (AoS, [n][3N+12]) by nsteps steps of size dt (loop.c:12-21 ->

@@ -24,7 +24,8 @@ typedef struct cfg {
   int N, neq, ncons, i0, i1, i2, i3, i4, i5, order, rk_steps, prelax, nsolids;
   int zerou[3];
   int flux_form;
-  double gamma[MAXN], pinf[MAXN], mu[MAXN], amin, avf_lim, dt;
+  int plastic;
+  double gamma[MAXN], pinf[MAXN], mu[MAXN], yield[MAXN], amin, avf_lim, dt;
   double lim[MAXNEQ];
 } cfg;
 
@@ -1011,6 +1012,109 @@ static void rk_update(const cfg *k, const ffvo_mesh *m, double *S, const work *W
 
 /* m5_relaxation_solid.c:3-40.  phi_new is set there only for solid materials; for a fluid
  * material 0 the reference reads it uninitialised -- here it keeps phi_old (no trigger). */
+/* ------------------------------------------------------------ radial-return plasticity */
+/* Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations (Golub & Van
+ * Loan, Matrix Computations, sec. 8.5): G = Q diag(lam) Q^T, Q's columns the eigenvectors. */
+static void jacobi3(const double G[9], double lam[3], double Q[9]) {
+  double a[3][3];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      a[i][j] = G[3 * i + j];
+      Q[3 * i + j] = (i == j) ? 1.0 : 0.0;
+    }
+  for (int sweep = 0; sweep < 32; sweep++) {
+    const double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+    const double dg = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+    if (!(off > 1e-32 * dg)) break;
+    for (int p = 0; p < 2; p++)
+      for (int q = p + 1; q < 3; q++) {
+        if (a[p][q] == 0.0) continue;
+        const double theta = (a[q][q] - a[p][p]) / (2.0 * a[p][q]);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        for (int r = 0; r < 3; r++) { /* a <- a J (columns p, q) */
+          const double arp = a[r][p], arq = a[r][q];
+          a[r][p] = c * arp - s * arq;
+          a[r][q] = s * arp + c * arq;
+        }
+        for (int r = 0; r < 3; r++) { /* a <- J^T a (rows p, q) */
+          const double apr = a[p][r], aqr = a[q][r];
+          a[p][r] = c * apr - s * aqr;
+          a[q][r] = s * apr + c * aqr;
+        }
+        for (int r = 0; r < 3; r++) { /* Q <- Q J */
+          const double qp = Q[3 * r + p], qq = Q[3 * r + q];
+          Q[3 * r + p] = c * qp - s * qq;
+          Q[3 * r + q] = s * qp + c * qq;
+        }
+      }
+  }
+  for (int i = 0; i < 3; i++) lam[i] = a[i][i];
+}
+
+/* von Mises stress of the hyperelastic deviator (state_equation.c:143-204, the mu term) for
+ * principal values g_i = exp(2 (m + beta d_i)) of G: s_i = -mu |G|^(-1/6) (t_i - mean t),
+ * t_i = g_i^2 - |G|^(1/3) g_i, |G| = exp(6 m) */
+static double vm_principal(double mu, double m, const double d[3], double beta) {
+  const double g13 = exp(2.0 * m), g16 = exp(m);
+  double t[3];
+  for (int i = 0; i < 3; i++) {
+    const double g = exp(2.0 * (m + beta * d[i]));
+    t[i] = g * g - g13 * g;
+  }
+  const double tm = (t[0] + t[1] + t[2]) / 3.0;
+  double j = 0.0;
+  for (int i = 0; i < 3; i++) {
+    const double s = -mu / g16 * (t[i] - tm);
+    j += s * s;
+  }
+  return sqrt(1.5 * j);
+}
+
+/* J2 radial return of a cell's deformation tensor A (no counterpart in the reference):
+ * with G = A A^T = Q diag(lam) Q^T, the Hencky strain h_i = ln(lam_i) / 2 splits into its
+ * mean m (volume, kept) and deviator d_i; where a solid's von Mises stress exceeds its
+ * yield stress, the deviator is scaled by the largest beta in [0, 1] (60 bisection steps)
+ * whose stress lies on or inside the yield surface, A <- Q diag(exp((beta - 1) d_i)) Q^T A.
+ * The total energy and the materials' alpha rho e are kept: the elastic energy released is
+ * dissipated into the materials' internal energy (the pressure recovery subtracts e_el from
+ * alpha rho e).  Returns 1 when A changed. */
+static int plastic_return(const cfg *k, double *s) {
+  double *A = s + k->i5, G[9], Gmag, lam[3], Q[9];
+  gmat_of(A, G, &Gmag);
+  jacobi3(G, lam, Q);
+  if (!(lam[0] > 0.0 && lam[1] > 0.0 && lam[2] > 0.0)) return 0;
+  double h[3], d[3];
+  for (int i = 0; i < 3; i++) h[i] = 0.5 * log(lam[i]);
+  const double m = (h[0] + h[1] + h[2]) / 3.0;
+  for (int i = 0; i < 3; i++) d[i] = h[i] - m;
+  double beta = 1.0;
+  for (int v = 0; v < k->N; v++) {
+    if (k->mu[v] == 0.0 || !(k->yield[v] > 0.0)) continue;
+    if (vm_principal(k->mu[v], m, d, beta) <= k->yield[v]) continue;
+    double lo = 0.0, hi = beta;
+    for (int it = 0; it < 60; it++) {
+      const double mid = 0.5 * (lo + hi);
+      if (vm_principal(k->mu[v], m, d, mid) <= k->yield[v]) lo = mid;
+      else hi = mid;
+    }
+    beta = lo;
+  }
+  if (beta == 1.0) return 0;
+  double M[9], An[9];
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) {
+      double x = 0.0;
+      for (int q = 0; q < 3; q++) x += Q[3 * i + q] * exp((beta - 1.0) * d[q]) * Q[3 * j + q];
+      M[3 * i + j] = x;
+    }
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++)
+      An[3 * i + j] = M[3 * i + 0] * A[0 + j] + M[3 * i + 1] * A[3 + j] + M[3 * i + 2] * A[6 + j];
+  for (int q = 0; q < 9; q++) A[q] = An[q];
+  return 1;
+}
+
 static int relaxation_solid(const cfg *k, const ffvo_mesh *m, double *S, const work *W) {
   const int neq = k->neq, N = k->N;
   for (int64_t c = 0; c < m->n; c++) {
@@ -1019,6 +1123,10 @@ static int relaxation_solid(const cfg *k, const ffvo_mesh *m, double *S, const w
     for (int iv = 0; iv < N - 1; ++iv) phi_old[iv] = s[k->i3 + iv] - k->avf_lim;
     int err = relaxationvec(k, s);
     if (err) return err;
+    /* the plastic step of the reference's prototype (m5_relaxation_solid.c:14 runs it per
+       leaf in this loop), after the relaxation so that the stored state lies on or inside
+       the yield surface (the relaxation scales A by the solid-fraction ratio) */
+    if (k->plastic) plastic_return(k, s);
     for (int iv = 0; iv < N - 1; ++iv)
       phi_new[iv] = (k->mu[iv] != 0.0) ? s[k->i3 + iv] - k->avf_lim : phi_old[iv];
     if (phi_old[0] * phi_new[0] < 0.0) gfm_fix(k, m, S, W, c, 1);
@@ -1049,7 +1157,9 @@ static int make_cfg(const ffvo_m5_params *p, double dt, cfg *k) {
     k->gamma[i] = p->gamma[i];
     k->pinf[i] = p->pinf[i];
     k->mu[i] = p->mu[i];
+    k->yield[i] = p->yield[i];
     if (p->mu[i] != 0.0) k->nsolids++;
+    if (p->mu[i] != 0.0 && p->yield[i] > 0.0) k->plastic = 1;
   }
   if (k->nsolids > 2) return 10;
   k->amin = p->amin;

@@ -32,7 +32,8 @@ class _M5Params(ctypes.Structure):
                 ("prelax", ctypes.c_int32), ("zerou", ctypes.c_int32 * 3),
                 ("flux_form", ctypes.c_int32), ("gamma", ctypes.c_double * 4),
                 ("pinf", ctypes.c_double * 4), ("mu", ctypes.c_double * 4),
-                ("amin", ctypes.c_double), ("avf_lim", ctypes.c_double)]
+                ("amin", ctypes.c_double), ("avf_lim", ctypes.c_double),
+                ("yield_", ctypes.c_double * 4)]
 
 
 def build() -> str:
@@ -107,6 +108,8 @@ def m5_advance(mesh: OracleMesh, S_aos: np.ndarray, dt: float, nsteps: int, m5: 
     p.zerou[:] = zerou
     for i, (g, q, mu) in enumerate(zip(m5["gamma"], m5["pinf"], m5["mu"])):
         p.gamma[i], p.pinf[i], p.mu[i] = g, q, mu
+    for i, y in enumerate(m5.get("yield", ())):
+        p.yield_[i] = y
     err = lib().ffvo_m5_advance(ctypes.byref(mesh.c), ctypes.byref(p), S.ctypes.data, dt, nsteps)
     if err:
         raise RuntimeError(f"oracle stopped with code {err} (the reference would exit here)")

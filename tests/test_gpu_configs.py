@@ -42,7 +42,8 @@ def test_fp64_small_config_matches_oracle(workload, flux_form, built_lib, oracle
     out = s.download_state()
     s.close()
     m5 = dict(avf_lim=kw["avf_lim"], prelax=kw["prelax"], amin=kw["amin"], pinf=list(kw["pinf"]),
-              gamma=list(kw["gamma"]), mu=list(kw["mu"]), flux_form=flux_form)
+              gamma=list(kw["gamma"]), mu=list(kw["mu"]), flux_form=flux_form,
+              **{"yield": list(kw.get("yield_stress") or ())})
     ref = pyoracle.m5_advance(pyoracle.OracleMesh(mesh.export()), S0.T, dt, 3, m5).T
     scale = np.maximum(np.abs(ref).max(axis=1), 1e-300)
     err = np.abs(out - ref).max(axis=1) / scale
@@ -100,4 +101,4 @@ def test_tags_on_small_config_match_restatement(workload, flux_form, built_lib):
     assert np.array_equal(si[0], SI[0]) and np.array_equal(si[1], SI[1])
     assert np.array_equal(raw, raw_r), np.flatnonzero(raw != raw_r)[:10]
     assert np.array_equal(split, split_r)
-    assert (raw > mesh.level).any()  # the criterion asks for refinement somewhere
+    assert len(np.unique(raw)) > 1  # the criterion sets more than one level
