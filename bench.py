@@ -1,18 +1,19 @@
 #!/usr/bin/env python3
 """Throughput benchmark of the explicit FV step (cell-updates per second).
 
-Default workload (--workload config3): gas-bubble collapse near a hyperelastic wall -- the
+Default workload (--workload config3): gas-bubble collapse near an elastoplastic wall -- the
 half-space z < 0.2 a solid (rho 2700, stiffened-gas gamma 3.5, p_inf 3.2e10, shear modulus
-2.6e10), above it liquid (gamma 4.4, p_inf 6e8, rho 1000, p 5e6) around a gas sphere (gamma
-1.4, rho 1, p 1e5) of radius 0.1 at 1.5 radii above the wall with a tanh interface over two
-finest cells; 2^3 trees refined from level 4 to level 9 around the wall and the bubble
-(10.1 M cells), transmissive sides; model 5 with 3 materials (NEQ 21), MUSCL-HLLC with
-face-state relaxation, ghost-fluid coupling at the solid (AVF_LIM 0.5), PRELAX 3, RK_STEPS 2.
-dt is CFL 0.01 on the solid's sound speed at the finest cell: the reference's model-5 scheme
-goes non-finite on this problem within 15-20 steps at CFL 0.03 (its own C code, reproduced
-bit for bit by the oracle).  Before timing, the reference's meshadaptation with the
-configuration's criteria (relative density jump, interface layers) adapts the mesh, and
-both timed loops start from that mesh and state.
+2.6e10, von Mises yield stress 3e8 Pa with a J2 radial return), above it liquid (gamma 4.4,
+p_inf 6e8, rho 1000, p 5e6) around a gas sphere (gamma 1.4, rho 1, p 1e5) of radius 0.1 at
+1.5 radii above the wall with a tanh interface over two finest cells; 2^3 trees refined from
+level 4 to level 9 around the wall and the bubble (10.1 M cells), transmissive sides; model 5
+with 3 materials (NEQ 21), MUSCL-HLLC with face-state relaxation, ghost-fluid coupling at the
+solid (AVF_LIM 0.5), PRELAX 3, RK_STEPS 2.  Model 5's flux is the consistent form by default
+(--flux-form; include/ffv.h FFV_FLUX_CONSISTENT: the reference's star-state energy and two flux
+signs made consistent with the rest of its HLLC solver), dt CFL 0.1 on the solid's sound
+speed at the finest cell.  Before timing, the reference's meshadaptation with the
+configuration's criteria (relative density jump, interface layers) adapts the mesh (9.5 M
+cells), and every timed loop starts from that mesh and state.
 
 One benchmark step is one time step (all RK stages) over the whole mesh; one cell-update
 is one cell advanced one time step.
@@ -21,21 +22,29 @@ is one cell advanced one time step.
              the time loop (network every step, the plain criterion as judge every 8 steps,
              regrids when it finds cells to refine), CUDA events on the solver's stream
              around the loop (judges and regrids included); state resident in HBM
+  accuracy_gate  the metric's condition at the timed step count (relative L1 of density and
+             the peak wall stress error, each <= 1e-4): the FP32-flux form against the FP64
+             form, the headline run against the comparator, and the medium wall mesh whose wall
+             is loaded within the window; pass/fail per quantity
   plain_fp64_amr  the comparator: plain FP64 with the reference's AMR (meshadaptation
              every 8 steps) over the same steps
   plain_fp64_form  plain FP64 steps alone (graph-launched, events around every step)
+  fp32_flux_form / reference_flux_form  the FP32-flux form alone, its error growth against
+             the FP64 form, in the consistent form and with the reference's own flux (the
+             latter at CFL 0.01, where the reference's scheme runs at all)
   e2e        the learned loop through the public API with host buffers: every step
              uploads the state from pinned host memory and downloads it after
   roofline   the dominant kernel's algorithmic bytes per launch over its mean duration,
              per-kernel CUDA events on the solver's stream (ffv_profile_stage)
-  cpu_baseline  the oracle's C restatement of the reference algorithm, one core, on a
-             bounded sample (same physics, smaller mesh)
+  cpu_baseline  the oracle's C restatement of the reference algorithm on all host cores, on
+             contiguous Morton ranges of the same mesh (generated in numpy; no library of the
+             product mapped)
 
-`--workload config2` is the two-phase bubble without the wall (2.30 M cells, plain FP64
-headline), `config1` the 32^3 Sod problem of model 0; `config2m` / `config3m` are the
-medium sizes used for profiler captures.  `--impl reference` times the reference algorithm
-on the host cores instead (the C restatement in oracle/, one process per core, each on the
-same bounded sample).
+`--workload config2` is the two-phase bubble without the wall (2.30 M cells), `config5` the
+64-bubble stress test (40.8 M cells), `config1` the 32^3 Sod problem of model 0; `config2m` /
+`config3m` / `config5m` are medium sizes.  `--impl reference` times the reference algorithm on
+the host cores instead (the C restatement in oracle/, one process per core, each on its own
+Morton range of the stated workload's mesh per round).
 """
 from __future__ import annotations
 
@@ -96,6 +105,12 @@ BUBBLE_SIZES = {"config2": (4, 8, 22.0), "config2m": (4, 7, 12.0), "config2s": (
 # 64-bubble stress test: (base level, finest level)
 FIELD_SIZES = {"config5": (8, 10), "config5m": (6, 8), "config5s": (4, 6)}
 FLUX_FORMS = {"reference": 0, "consistent": 1}
+# CFL number of the wall configurations (dt on the solid's sound speed at the finest cell):
+# with the consistent flux form and the radial return the medium wall mesh runs 400 steps at
+# 0.1; the reference's own flux goes non-finite within ~20 steps at 0.03, so its legs take
+# REFERENCE_FLUX_CFL
+WALL_CFL = 0.1
+REFERENCE_FLUX_CFL = 0.01
 FLUX_FORM_NOTE = {
     0: "the reference's m5 flux as written (m5_star_region.c:59, m5_flux.c:20-34, 53-56)",
     1: "consistent: Rankine-Hugoniot star-state energy and m5_flux_gfm.c's momentum and "
@@ -120,7 +135,7 @@ def workload_config(workload: str, n: int | None = None, levels=None) -> dict:
                             f"(3 materials), levels 4-{lmax} AMR; FP32-flux + learned AMR against "
                             "plain FP64 + AMR; MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
                 "cells": n, "levels": levels, "neq": 21,
-                "dt": 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": 0.01,
+                "dt": WALL_CFL * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": WALL_CFL,
                 "cfl_speed": "solid sound speed, finest cell", "parallelism": "single GPU",
                 "l2": f"state {8 * 21 * n / 1e6:.0f} MB > L2 (129 MB): no flush needed"}
     if workload.startswith("config5"):
@@ -132,7 +147,7 @@ def workload_config(workload: str, n: int | None = None, levels=None) -> dict:
                             "at the interfaces, model 5 (3 materials); FP32-flux + learned AMR "
                             "against plain FP64 + AMR; MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
                 "cells": n, "levels": levels, "neq": 21,
-                "dt": 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": 0.01,
+                "dt": WALL_CFL * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": WALL_CFL,
                 "cfl_speed": "solid sound speed, finest cell", "parallelism": "single GPU",
                 "l2": f"state {8 * 21 * n / 1e6:.0f} MB > L2 (129 MB): no flush needed"}
     lmin, lmax, _ = BUBBLE_SIZES[workload]
@@ -363,12 +378,12 @@ def cpu_case(workload: str):
         lmax, band = WALL_SIZES[workload]
         lv, state = W.bubble_wall_parts(lmax=lmax, band_cells=band)
         kw = _wall_solver_kwargs(W.WALL)
-        dt = 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID
+        dt = WALL_CFL * (0.5 / (1 << (lmax - 1))) / C_SOLID
     elif workload.startswith("config5"):
         lbase, lmax = FIELD_SIZES[workload]
         lv, state, _, _ = W.bubble_field_parts(lbase=lbase, lmax=lmax)
         kw = _wall_solver_kwargs(W.WALL)
-        dt = 0.01 * (0.5 / (1 << (lmax - 1))) / C_SOLID
+        dt = WALL_CFL * (0.5 / (1 << (lmax - 1))) / C_SOLID
     else:
         lmin, lmax, band = BUBBLE_SIZES[workload]
         lv, state = W.bubble_config2_parts(lmin=lmin, lmax=lmax, band_cells=band)
@@ -622,7 +637,7 @@ def train_wall_indicator(kw: dict, dev, amr_cfg: dict, seed: int = 20261203):
     rng = np.random.default_rng(seed)
     ind = Indicator(device=dev.index, seed=seed)
     tags7 = wall_tags(7)
-    dt7 = 0.01 * (0.5 / (1 << 6)) / C_SOLID
+    dt7 = WALL_CFL * (0.5 / (1 << 6)) / C_SOLID
     Xs, ys, runs = [], [], 0
     for k in range(3):
         standoff, radius = rng.uniform(1.0, 2.5), rng.uniform(0.05, 0.15)
@@ -859,11 +874,13 @@ def run_ours(args) -> None:
             s64 = Solver(device=local, **kref)
             s64.set_mesh(mesh)
             s64.upload_state(S0)
-            rf = measure_fp32_form(mesh, S0, dt, kref, args, dev, s64)
+            dt_ref = dt * REFERENCE_FLUX_CFL / cfg.get("cfl", REFERENCE_FLUX_CFL)
+            rf = measure_fp32_form(mesh, S0, dt_ref, kref, args, dev, s64)
             s64.close()
             line["reference_flux_form"] = {k: rf[k] for k in (
                 "value", "ms_per_step", "flux_form", "error_vs_fp64", "gate",
                 "fp64_sensitivity_floor", "error_growth")}
+            line["reference_flux_form"]["cfl"] = REFERENCE_FLUX_CFL
         line["clocks"] = clocks.stop()
         print(json.dumps(line), flush=True)
     else:

@@ -76,12 +76,16 @@ __device__ inline double plastic_vm(double mu, double m, const double d[3], doub
 __device__ inline float plastic_vm_screen(const double *A, float mu) {
   float a[9], G[9];
   for (int q = 0; q < 9; q++) a[q] = (float)A[q];
+  // a fluid cell carries A = 0 (G = 0, no elastic stress): nothing to screen
+  if (a[0] == 0.0f && a[4] == 0.0f && a[8] == 0.0f && a[1] == 0.0f && a[2] == 0.0f &&
+      a[3] == 0.0f && a[5] == 0.0f && a[6] == 0.0f && a[7] == 0.0f)
+    return 0.0f;
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++)
       G[3 * i + j] = a[3 * i] * a[3 * j] + a[3 * i + 1] * a[3 * j + 1] + a[3 * i + 2] * a[3 * j + 2];
   const float det = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
                     G[2] * (G[3] * G[7] - G[4] * G[6]);
-  if (!(det > 0.0f)) return 0.0f;
+  if (!(det > 0.0f)) return 0.0f;  // fluid cells (A = 0): no elastic stress
   const float g13 = cbrtf(det), g16 = sqrtf(g13);
   float t[9];
   for (int i = 0; i < 3; i++)

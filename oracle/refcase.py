@@ -34,7 +34,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(HERE, "_ref", "forestfv_ref")
-REF_SRC = "/root/reference/src/c"
+# the reference's C sources, read where they lie (FFV_REFERENCE_SRC, or the checkout's place
+# in this build container); absent on machines without the reference
+REF_SRC = os.environ.get("FFV_REFERENCE_SRC", "/root/reference/src/c")
 
 # corner k of a hex tree/child -> (x, y, z) bit positions
 LAYOUT_INWARD = ((1, 0, 2),)   # x = bit1, y = bit0, z = bit2
