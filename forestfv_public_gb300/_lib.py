@@ -76,7 +76,7 @@ class TagParams(ctypes.Structure):
 
 
 EXPORTS = (
-    "ffv_mesh_build", "ffv_mesh_ncells", "ffv_mesh_free", "ffv_mesh_export", "ffv_create",
+    "ffv_mesh_build", "ffv_mesh_build_part", "ffv_mesh_ncells", "ffv_mesh_free", "ffv_mesh_export", "ffv_create",
     "ffv_destroy", "ffv_set_mesh", "ffv_upload_state", "ffv_download_state", "ffv_stage",
     "ffv_step", "ffv_sync", "ffv_cfl_dt", "ffv_state_device_ptr", "ffv_launches_per_step",
     "ffv_error_string", "ffv_stream", "ffv_profile_stage", "ffv_stage_kernel_name", "ffv_step_async",
@@ -100,6 +100,8 @@ def lib() -> ctypes.CDLL:
     vp, i32, i64, dbl = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
     L.ffv_mesh_build.argtypes = [ctypes.POINTER(ForestDesc), i64, vp, vp, vp,
                                  ctypes.POINTER(vp), vp]
+    L.ffv_mesh_build_part.argtypes = [ctypes.POINTER(ForestDesc), i64, vp, vp, vp,
+                                      ctypes.POINTER(vp), vp]
     L.ffv_mesh_ncells.argtypes = [vp]
     L.ffv_mesh_ncells.restype = i64
     L.ffv_mesh_free.argtypes = [vp]

@@ -157,9 +157,12 @@ struct CellMap {
 
 }  // namespace
 
-extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
-                              const int32_t *tree_ijk, const int32_t *level,
-                              const int32_t *cell_ijk, ffv_mesh **out, int64_t *order_out) {
+// part: the leaves are a part of a forest (one rank's cells and halo): a face whose
+// neighbour, or any of whose four finer neighbours, is not among them becomes a transmissive
+// boundary face instead of an error
+static int mesh_build(const ffv_forest_desc *desc, int64_t nleaves, const int32_t *tree_ijk,
+                      const int32_t *level, const int32_t *cell_ijk, ffv_mesh **out,
+                      int64_t *order_out, bool part) {
   if (!desc || !tree_ijk || !level || !cell_ijk || !out || nleaves <= 0) return FFV_ERR_ARG;
   if (nleaves > (int64_t)INT32_MAX / 8) return FFV_ERR_ARG;
   *out = nullptr;
@@ -380,6 +383,11 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
               ids[k] = where.get(cell_key(l + 1, fg[0], fg[1], fg[2]));
               ok = ids[k] >= 0;
             }
+            if (!ok && part) {
+              info |= (FFV_FK_BC | (uint32_t)FFV_BC_OUTLET) << (4 * f);
+              m->nbr[6 * c + f] = -1;
+              continue;
+            }
             if (!ok) {
               // distinguish a 2:1 violation (deeper leaves behind the face) from a hole
               bool deeper = false;
@@ -444,6 +452,18 @@ extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
   if (!sub.empty()) memcpy(m->sub, sub.data(), sizeof(int32_t) * sub.size());
   *out = m;
   return FFV_OK;
+}
+
+extern "C" int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves,
+                              const int32_t *tree_ijk, const int32_t *level,
+                              const int32_t *cell_ijk, ffv_mesh **out, int64_t *order_out) {
+  return mesh_build(desc, nleaves, tree_ijk, level, cell_ijk, out, order_out, false);
+}
+
+extern "C" int ffv_mesh_build_part(const ffv_forest_desc *desc, int64_t nleaves,
+                                   const int32_t *tree_ijk, const int32_t *level,
+                                   const int32_t *cell_ijk, ffv_mesh **out, int64_t *order_out) {
+  return mesh_build(desc, nleaves, tree_ijk, level, cell_ijk, out, order_out, true);
 }
 
 int64_t ffv_sibling_group(const ffv_mesh *m, int64_t c) {

@@ -74,7 +74,10 @@ def morton_tree_order(ntrees) -> np.ndarray:
 class Mesh:
     """Owner-sorted face tables built by the library (ffv_mesh_build)."""
 
-    def __init__(self, ntrees, leaves: Leaves, bc=(BC_OUTLET,) * 6, tree_edge: float | None = None):
+    def __init__(self, ntrees, leaves: Leaves, bc=(BC_OUTLET,) * 6, tree_edge: float | None = None,
+                 part: bool = False):
+        """part: the leaves are a part of a forest (ffv_mesh_build_part): faces towards
+        leaves that are not among them become transmissive boundaries."""
         L = _lib.lib()
         self.ntrees = tuple(int(t) for t in ntrees)
         self.bc = tuple(int(b) for b in bc)
@@ -88,8 +91,9 @@ class Mesh:
         cij = np.ascontiguousarray(leaves.cell_ijk, dtype=np.int32)
         self._order = np.zeros(leaves.n, dtype=np.int64)
         h = ctypes.c_void_p()
-        _lib.check(L.ffv_mesh_build(ctypes.byref(d), leaves.n, tij.ctypes.data, lev.ctypes.data,
-                                    cij.ctypes.data, ctypes.byref(h), self._order.ctypes.data),
+        build = L.ffv_mesh_build_part if part else L.ffv_mesh_build
+        _lib.check(build(ctypes.byref(d), leaves.n, tij.ctypes.data, lev.ctypes.data,
+                         cij.ctypes.data, ctypes.byref(h), self._order.ctypes.data),
                    "ffv_mesh_build")
         self._h = h
         self.n = int(L.ffv_mesh_ncells(h))

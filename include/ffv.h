@@ -141,6 +141,15 @@ typedef struct ffv_ctx ffv_ctx;   /* device context */
 int ffv_mesh_build(const ffv_forest_desc *desc, int64_t nleaves, const int32_t *tree_ijk,
                    const int32_t *level, const int32_t *cell_ijk, ffv_mesh **out,
                    int64_t *order_out);
+/* ffv_mesh_build for a part of a forest -- one rank's cells and their halo under a Morton-range
+ * partition (replaces the proxy layer the reference builds per rank, rebuildprox.c:3-246,
+ * restructtopo.c:3-14): a face whose neighbour, or any of whose four finer neighbours, is not
+ * among the leaves becomes a transmissive boundary face (FFV_BC_OUTLET) instead of an error.
+ * The halo cells next to such faces compute with a stand-in neighbour; a halo deep enough for
+ * the cells a rank owns keeps those exact (forestfv_public_gb300/partition.py). */
+int ffv_mesh_build_part(const ffv_forest_desc *desc, int64_t nleaves, const int32_t *tree_ijk,
+                        const int32_t *level, const int32_t *cell_ijk, ffv_mesh **out,
+                        int64_t *order_out);
 int64_t ffv_mesh_ncells(const ffv_mesh *m);
 void ffv_mesh_free(ffv_mesh *m);
 
