@@ -178,3 +178,34 @@ def test_fields_match_host_eos(built_lib):
     assert np.all(F[4][ref["vm"] == 0.0] == 0.0)
     ind.close()
     s.close()
+
+
+@pytest.mark.parametrize("threshold", [0.2, 0.5])
+def test_fused_marks_equal_gather_then_forward(threshold, built_lib):
+    """ffv_mlp_mark (features built in shared memory, forward and marks in one kernel) gives
+    the marks of ffv_mlp_predict (features through global memory, then the forward kernel):
+    the same probabilities against the threshold, accumulation OR-ing into earlier marks."""
+    g = load_golden("m5_wall_amr")
+    m = mesh_from_golden(g)
+    q = m5_params(g)
+    s = Solver(model=5, gamma=q["gamma"], pinf=q["pinf"], mu=q["mu"], amin=q["amin"],
+               avf_lim=q["avf_lim"], prelax=q["prelax"])
+    s.set_mesh(m)
+    s.upload_state(np.ascontiguousarray(g["S_final"].T))
+    ind = Indicator(seed=5)
+    ind.set_params(random_params(np.random.default_rng(9)))
+    F = ind.fields(s).cpu().numpy().astype(np.float64)
+    ind.set_norm(F.mean(axis=1), F.std(axis=1) + 1e-3)
+    p = ind.predict(s)
+    assert 0 < (p > threshold).sum() < m.n  # both outcomes occur
+    marks = torch.zeros(m.n, dtype=torch.uint8, device="cuda")
+    ind.mark(s, threshold, marks, accumulate=False)
+    s.sync()
+    assert np.array_equal(marks.cpu().numpy(), (p > threshold).astype(np.uint8))
+    prior = torch.from_numpy((np.arange(m.n) % 7 == 0).astype(np.uint8)).cuda()
+    ind.mark(s, threshold, prior, accumulate=True)
+    s.sync()
+    assert np.array_equal(prior.cpu().numpy(),
+                          ((p > threshold) | (np.arange(m.n) % 7 == 0)).astype(np.uint8))
+    ind.close()
+    s.close()
