@@ -966,6 +966,73 @@ def measure_amr(mesh, S0, dt, kw, args, dev, amr_cfg, alg_bytes, roofline_of, ke
     return out
 
 
+def run_stress(args) -> None:
+    """The stress test (config5, 40.8 M cells): one solver context at a time (a context holds
+    ~145 GB of device buffers at this size, so the legs that keep two or three alive do not
+    fit): the plain FP64 form, then the FP32-flux form, each timed with CUDA events on its
+    stream over `steps` steps after `warmup`, its per-kernel times, and the FP32 form's
+    error against the FP64 form after the same steps from host copies of both states."""
+    import torch
+
+    from forestfv_public_gb300 import Solver
+    from forestfv_public_gb300.fields import error_report
+    dev = torch.device("cuda", 0)
+    mesh, S0, dt, cfg, kw, alg_bytes, _ = WORKLOADS[args.workload]()
+    flux_form = FLUX_FORMS[args.flux_form]
+    kw["flux_form"] = flux_form
+    cfg["flux_form"] = FLUX_FORM_NOTE[flux_form]
+    out = {}
+    clocks = ClockSampler()
+    clocks.start()
+    for name, precision in (("plain_fp64_form", 0), ("fp32_flux_form", 1)):
+        s = Solver(device=0, precision=precision, **kw)
+        s.set_mesh(mesh)
+        s.upload_state(S0)
+        stream = torch.cuda.ExternalStream(s.stream_handle(), device=dev)
+        s.step(dt, args.warmup)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+        s.step_async(dt, args.steps)
+        e1.record(stream)
+        s.sync()
+        torch.cuda.synchronize(dev)
+        t_ms = e0.elapsed_time(e1)
+        per = {}
+        for _ in range(2):
+            for irk in (1, 2):
+                for k, v in s.profile_stage(irk, dt).items():
+                    per.setdefault(k, []).append(v)
+        mean_ms = {k: sum(v) / len(v) for k, v in per.items()}
+        dom = max(mean_ms, key=mean_ms.get)
+        peak, peak_kind = peak_hbm()
+        achieved = alg_bytes.get(dom, 0) * mesh.n / (mean_ms[dom] / 1e3) / 1e9
+        out[name] = {"value": mesh.n * args.steps / (t_ms / 1e3), "unit": UNIT,
+                     "ms_per_step": t_ms / args.steps, "kernel_mean_ms_per_stage": mean_ms,
+                     "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved,
+                                  "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                                  "traffic": ncu_summary(dom, mesh.n, "config3")[0],
+                                  "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"},
+                     "gpu_launches": s.launches_per_step() * args.steps}
+        out[name]["state"] = s.download_state()
+        s.close()
+    e = error_report(out["fp32_flux_form"].pop("state"), out["plain_fp64_form"].pop("state"),
+                     kw["gamma"], kw["pinf"], kw["mu"], kw["amin"], 0)
+    out["fp32_flux_form"]["error_vs_fp64"] = e
+    out["fp32_flux_form"]["gate"] = accuracy_gate(e, args.steps + args.warmup, kw.get("mu"))
+    f32, f64 = out["fp32_flux_form"], out["plain_fp64_form"]
+    line = {"metric": METRIC, "value": f32["value"], "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": f32["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 flux, f64 state and residuals", "data": "synthetic", "config": cfg,
+            "form": "FP32-flux form (no AMR loop: one solver context at a time at this size)",
+            "roofline": f32["roofline"], "gpu_launches": f32["gpu_launches"],
+            "speedup_vs_plain_fp64": f32["value"] / f64["value"],
+            "plain_fp64_form": f64, "fp32_flux_form": f32, "clocks": clocks.stop()}
+    print(json.dumps(line), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -979,6 +1046,9 @@ def main() -> None:
                     help="model 5's flux: the reference's as written, or made consistent "
                          "(include/ffv.h FFV_FLUX_CONSISTENT); the default is the one whose "
                          "FP32-flux form meets the metric's accuracy condition")
+    ap.add_argument("--loops", action="store_true",
+                    help="config5: the full set of legs (AMR loops, error-growth solvers side by "
+                         "side) instead of the one-context-at-a-time stress leg")
     ap.add_argument("--no-reference-form", action="store_true",
                     help="skip the FP32-flux error report with the reference's own flux")
     ap.add_argument("--no-amr", action="store_true",
@@ -990,6 +1060,8 @@ def main() -> None:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload.startswith("config5") and not args.loops:
+        run_stress(args)
     else:
         run_ours(args)
 
