@@ -479,74 +479,6 @@ __global__ void __launch_bounds__(TPB) mlp_train_kernel(const bf16 *__restrict__
 
 // AdamW (decoupled weight decay on W1, W2, w3; none on the biases)
 // marks[c] = (accumulate ? marks[c] : 0) | (prob[c] > threshold)
-// The network on the context's state, fused: each warp builds the feature rows of its 16 cells
-// straight into its shared tile -- the same 27-cell stencil walk and normalisation as
-// mlp_gather, lanes over (row, stencil cell) pairs -- runs the forward pass on the tensor cores
-// and writes the marks.  The feature rows (288 bytes a cell) never go to global memory.
-__global__ void __launch_bounds__(TPB) mlp_mark_fused(ffv_dmesh m, const float *__restrict__ F,
-                                                      const float *__restrict__ norm,
-                                                      const bf16 *__restrict__ W1,
-                                                      const bf16 *__restrict__ W2,
-                                                      const float *__restrict__ P,
-                                                      float threshold, uint8_t *__restrict__ marks,
-                                                      int accumulate) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const Smem s = carve(smem, false);
-  stage_weights(s, W1, W2, nullptr, P, false);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
-  bf16 *Xs = s.X + warp * 16 * SX, *H1s = s.H1 + warp * 16 * SH;
-  const float b3 = P[OFF_B3];
-  float mean[5], istd[5];
-#pragma unroll
-  for (int f = 0; f < 5; f++) {
-    mean[f] = norm[f];
-    istd[f] = 1.0f / norm[5 + f];
-  }
-  const int64_t ntiles = (m.n + 15) / 16;
-  for (int64_t t = (int64_t)blockIdx.x * WARPS + warp; t < ntiles; t += (int64_t)gridDim.x * WARPS) {
-    const int64_t r0 = t * 16;
-    const int valid = (int)((m.n - r0) < 16 ? (m.n - r0) : 16);
-#pragma unroll 1
-    for (int i = lane; i < 16 * 27; i += 32) {
-      const int r = i / 27, o = i - 27 * r;
-      bf16 *row = Xs + r * SX + 5 * o;
-      if (r < valid) {
-        const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = o / 9 - 1;
-        int64_t e = r0 + r;
-        if (dx) e = face_step(m, e, dx < 0 ? 0 : 2);
-        if (dy) e = face_step(m, e, dy < 0 ? 3 : 1);
-        if (dz) e = face_step(m, e, dz < 0 ? 4 : 5);
-#pragma unroll
-        for (int f = 0; f < 5; f++)
-          row[f] = __float2bfloat16_rn((F[(int64_t)f * m.n + e] - mean[f]) * istd[f]);
-      } else {
-#pragma unroll
-        for (int f = 0; f < 5; f++) row[f] = __float2bfloat16_rn(0.0f);
-      }
-    }
-    // the zero padding of every row, features 135..143
-    for (int i = lane; i < 16 * (KIN - NIN); i += 32)
-      Xs[(i / (KIN - NIN)) * SX + NIN + i % (KIN - NIN)] = __float2bfloat16_rn(0.0f);
-    __syncwarp();
-    float a1[8][4], a2[8][4], zg, zg8;
-    tile_forward(s, Xs, H1s, a1, a2, zg, zg8);
-    if (q == 0) {
-#pragma unroll
-      for (int h = 0; h < 2; h++) {
-        const int r = g + 8 * h;
-        if (r < valid) {
-          const float pr = 1.0f / (1.0f + expf(-((h ? zg8 : zg) + b3)));
-          const uint8_t hit = pr > threshold ? 1 : 0;
-          const int64_t c = r0 + r;
-          marks[c] = accumulate ? (uint8_t)(marks[c] | hit) : hit;
-        }
-      }
-    }
-    __syncwarp();
-  }
-}
-
 __global__ void mlp_mark(int64_t n, const float *__restrict__ prob, float threshold,
                          uint8_t *__restrict__ marks, int accumulate) {
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
@@ -852,14 +784,11 @@ int ffv_mlp_mark(ffv_ctx *ctx, ffv_mlp *m, float threshold, uint8_t *marks_dev,
   rc = ensure_cap(m, v.dm.n);
   if (rc != FFV_OK) return rc;
   launch_fields(v, m->d_F);
-  const size_t sb = smem_bytes(false);
-  MCK(cudaFuncSetAttribute(mlp_mark_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-  const int64_t tiles = (v.dm.n + 15) / 16;
-  int64_t blocks = (tiles + WARPS - 1) / WARPS;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  if (blocks < 1) blocks = 1;
-  mlp_mark_fused<<<(unsigned)blocks, TPB, sb, v.st>>>(v.dm, m->d_F, m->d_norm, m->d_W1, m->d_W2,
-                                                     m->d_P, threshold, marks_dev, accumulate);
+  mlp_gather<<<(unsigned)((v.dm.n + 127) / 128), 128, 0, v.st>>>(v.dm, m->d_F, m->d_norm, m->d_X);
+  MCK(cudaGetLastError());
+  rc = forward(m, m->d_X, v.dm.n, m->d_prob, v.st);
+  if (rc != FFV_OK) return rc;
+  mlp_mark<<<152 * 4, 256, 0, v.st>>>(v.dm.n, m->d_prob, threshold, marks_dev, accumulate);
   MCK(cudaGetLastError());
   return FFV_OK;
 }

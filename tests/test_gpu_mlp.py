@@ -181,10 +181,10 @@ def test_fields_match_host_eos(built_lib):
 
 
 @pytest.mark.parametrize("threshold", [0.2, 0.5])
-def test_fused_marks_equal_gather_then_forward(threshold, built_lib):
-    """ffv_mlp_mark (features built in shared memory, forward and marks in one kernel) gives
-    the marks of ffv_mlp_predict (features through global memory, then the forward kernel):
-    the same probabilities against the threshold, accumulation OR-ing into earlier marks."""
+def test_marks_equal_predicted_probabilities(threshold, built_lib):
+    """ffv_mlp_mark (on the device, nothing copied back) gives the marks of
+    ffv_mlp_predict's probabilities against the threshold, accumulation OR-ing into earlier
+    marks."""
     g = load_golden("m5_wall_amr")
     m = mesh_from_golden(g)
     q = m5_params(g)
