@@ -21,6 +21,9 @@
 //     material's recovered pressure (rounded once to FP32) and the last material's volume
 //     fraction (1 - sum formed on the pairs: in FP32 that difference would lose a 1e-6
 //     fraction next to 1).
+//   * The deformation tensor A is carried as its deviation D = A - I wherever it is FP32
+//     (copy of the state, face records, face states): the elastic stress and energy are
+//     formed from E = A A^T - I = D + D^T + D D^T, exact to FP32 relative to the strain.
 //   * Wave speeds, star region, physical flux, HLLC and its ghost-fluid variant: FP32.
 //     Face fluxes are stored as FP32 and summed into the FP64 cell residual by
 //     m5f_cell_update; the RK state stays FP64.
@@ -42,63 +45,102 @@ struct RecL {
 };
 
 // ------------------------------------------------------------------ EOS in FP32
-__device__ __forceinline__ void gmat_f(const float A[9], float G[9], float &Gmag) {
-  G[0] = A[0] * A[0] + A[1] * A[1] + A[2] * A[2];
-  G[1] = A[0] * A[3] + A[1] * A[4] + A[2] * A[5];
-  G[2] = A[0] * A[6] + A[1] * A[7] + A[2] * A[8];
-  G[3] = G[1];
-  G[4] = A[3] * A[3] + A[4] * A[4] + A[5] * A[5];
-  G[5] = A[3] * A[6] + A[4] * A[7] + A[5] * A[8];
-  G[6] = G[2];
-  G[7] = G[5];
-  G[8] = A[6] * A[6] + A[7] * A[7] + A[8] * A[8];
-  Gmag = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
-         G[2] * (G[3] * G[7] - G[4] * G[6]);
+// The FP32 form carries the deformation tensor as its deviation D = A - I from the identity
+// (the FP32 copy of the state, the face records, the face states).  The solid's stress is
+// mu times the strain, ~1e-3 beside the identity: G = A A^T formed from an FP32 A would carry
+// the ~6e-8 rounding of entries near 1 into every stress (mu * 1e-7, tens of kPa for a metal),
+// while E = G - I = D + D^T + D D^T keeps FP32 precision relative to the strain itself.
+// The reference's G-form expressions (state_equation.c:143-204, 269-317) are rewritten
+// exactly in E:  |G| - 1 = tr E + (sum of E's principal 2x2 minors) + det E,
+// tr((G - |G|^(1/3) I)^2) = tr((E - g I)^2) and the stress deviator
+// G^2 - tr(G^2)/3 I - |G|^(1/3) (G - tr G/3 I) = (1 - g) dev E + dev(E^2), g = |G|^(1/3) - 1.
+struct StrainF {
+  float E[6];  // G - I (symmetric): E00, E11, E22, E01, E02, E12
+  float g;     // |G|^(1/3) - 1
+  float g16;   // |G|^(1/6)
+  bool solid;  // |G| != 0 (a fluid cell carries A = 0: no elastic stress)
+};
+
+// slot of E_ij in StrainF::E
+__host__ __device__ constexpr int esym(int i, int j) {
+  return i == j ? i : (i + j == 1 ? 3 : (i + j == 2 ? 4 : 5));
+}
+
+__device__ __forceinline__ void strain_f(const float D[9], StrainF &s) {
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++)
+      s.E[esym(i, j)] = D[3 * i + j] + D[3 * j + i] +
+                        (D[3 * i] * D[3 * j] + D[3 * i + 1] * D[3 * j + 1] + D[3 * i + 2] * D[3 * j + 2]);
+  const float e00 = s.E[0], e11 = s.E[1], e22 = s.E[2], e01 = s.E[3], e02 = s.E[4], e12 = s.E[5];
+  const float m2 = (e00 * e11 - e01 * e01) + (e00 * e22 - e02 * e02) + (e11 * e22 - e12 * e12);
+  const float dE = e00 * (e11 * e22 - e12 * e12) - e01 * (e01 * e22 - e12 * e02) +
+                   e02 * (e01 * e12 - e11 * e02);
+  const float x = (e00 + e11 + e22) + m2 + dE;  // |G| - 1
+  s.solid = (1.0f + x) != 0.0f;
+  if (fabsf(x) <= 0.03125f) {
+    // (1 + x)^(1/3) - 1 by its binomial series to x^5 (coefficients 1/3, -1/9, 5/81,
+    // -10/243, 22/729); the first omitted term is below 2e-9 of the sum for |x| <= 1/32
+    s.g = x * (1.0f / 3.0f + x * (-1.0f / 9.0f + x * (5.0f / 81.0f + x * (-10.0f / 243.0f + x * (22.0f / 729.0f)))));
+    s.g16 = sqrtf(1.0f + s.g);
+  } else {
+    const float g13 = cbrtf(fabsf(1.0f + x));
+    s.g = g13 - 1.0f;
+    s.g16 = sqrtf(g13);
+  }
 }
 
 // e_el = mu / (4 |G|^(1/6)) tr((G - |G|^(1/3) I)^2)   (state_equation.c:269-317)
-__device__ __forceinline__ float elastic_energy_f(const float G[9], float Gmag, float mu) {
-  if (!(fabsf(Gmag) != 0.0f) || !(mu != 0.0f)) return 0.0f;
-  float g13 = cbrtf(fabsf(Gmag));
-  if (isnan(g13)) g13 = 0.0f;
-  const float d0 = G[0] - g13, d4 = G[4] - g13, d8 = G[8] - g13;
-  // tr(M^2) of the symmetric M = G - g13 I
-  const float tr = d0 * d0 + d4 * d4 + d8 * d8 + 2.0f * (G[1] * G[1] + G[2] * G[2] + G[5] * G[5]);
-  return mu / (4.0f * sqrtf(g13)) * tr;
+__device__ __forceinline__ float elastic_energy_f(const StrainF &s, float mu) {
+  if (!s.solid || !(mu != 0.0f)) return 0.0f;
+  const float *E = s.E;
+  const float d0 = E[0] - s.g, d1 = E[1] - s.g, d2 = E[2] - s.g;
+  const float tr = d0 * d0 + d1 * d1 + d2 * d2 + 2.0f * (E[3] * E[3] + E[4] * E[4] + E[5] * E[5]);
+  return mu / (4.0f * s.g16) * tr;
 }
 
-// material stress -alpha p I - mu/|G|^(1/6) (G^2 - tr(G^2)/3 I - |G|^(1/3)(G - tr G/3 I)),
-// accumulated into st (state_equation.c:143-204)
-__device__ __forceinline__ void eos_stress_f(float st[3][3], float avf, float pr, const float G[9],
-                                             float Gmag, float mu, float (*ast)[3]) {
-  float s[9];
-  if ((fabsf(Gmag) != 0.0f) && (mu != 0.0f)) {
-    float G2[9];
+// material stress -alpha p I - mu/|G|^(1/6) ((1 - g) dev E + dev(E^2)), accumulated into st
+// (state_equation.c:143-204 in the E form)
+__device__ __forceinline__ void eos_stress_f(float st[3][3], float avf, float pr, const StrainF &e,
+                                             float mu, float (*ast)[3]) {
+  float s[6];
+  if (e.solid && (mu != 0.0f)) {
+    const float *E = e.E;
+    float E2[6];
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int j = 0; j < 3; ++j)
-        G2[i * 3 + j] = G[i * 3 + 0] * G[0 * 3 + j] + G[i * 3 + 1] * G[1 * 3 + j] +
-                        G[i * 3 + 2] * G[2 * 3 + j];
-    const float J1 = G[0] + G[4] + G[8], J2 = G2[0] + G2[4] + G2[8];
-    const float p13 = cbrtf(fabsf(Gmag));
-    const float f = mu / sqrtf(p13);
+      for (int j = i; j < 3; j++)
+        E2[esym(i, j)] = E[esym(i, 0)] * E[esym(0, j)] + E[esym(i, 1)] * E[esym(1, j)] +
+                         E[esym(i, 2)] * E[esym(2, j)];
+    const float J1 = (E[0] + E[1] + E[2]) * (1.0f / 3.0f), J2 = (E2[0] + E2[1] + E2[2]) * (1.0f / 3.0f);
+    const float a = 1.0f - e.g;
+    const float f = mu / e.g16;
 #pragma unroll
-    for (int q = 0; q < 9; q++) {
-      const bool dg = (q == 0 || q == 4 || q == 8);
-      const float ss = dg ? G2[q] - J2 * (1.0f / 3.0f) - p13 * (G[q] - J1 * (1.0f / 3.0f))
-                          : G2[q] - p13 * G[q];
-      s[q] = dg ? -avf * pr - f * ss : -f * ss;
-    }
+    for (int q = 0; q < 6; q++)
+      s[q] = q < 3 ? -avf * pr - f * (a * (E[q] - J1) + (E2[q] - J2)) : -f * (a * E[q] + E2[q]);
   } else {
 #pragma unroll
-    for (int q = 0; q < 9; q++) s[q] = (q == 0 || q == 4 || q == 8) ? -avf * pr : 0.0f;
+    for (int q = 0; q < 6; q++) s[q] = q < 3 ? -avf * pr : 0.0f;
   }
 #pragma unroll
-  for (int q = 0; q < 9; q++) {
-    st[q / 3][q % 3] += s[q];
-    if (ast) ast[q / 3][q % 3] = s[q];
-  }
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+      st[i][j] += s[esym(i, j)];
+      if (ast) ast[i][j] = s[esym(i, j)];
+    }
+}
+
+// D of an FP64 deformation tensor: A - I formed in FP64, then rounded
+__device__ __forceinline__ float dev_of(const double *A, int q) {
+  return (float)(A[q] - ((q == 0 || q == 4 || q == 8) ? 1.0 : 0.0));
+}
+
+// A of a deviation, for the advection of A (there relative FP32 precision of A is enough)
+__device__ __forceinline__ float full_of(const float *D, int q) {
+  return D[q] + ((q == 0 || q == 4 || q == 8) ? 1.0f : 0.0f);
 }
 
 template <int N>
@@ -106,7 +148,7 @@ struct SolF {
   float r, u, v, w, e, ut, vt, wt, c2;
   float phi0;
   float ra[N], avf[N], are[N], p[N];
-  float A[9], st[3][3];
+  float D[9], st[3][3];  // D = A - I
   float vec[K5<N>::NC];
 };
 
@@ -137,9 +179,9 @@ __device__ void make_sol_f(const M5Consts &k, const float *U, float phi0, SolF<N
 #pragma unroll
   for (int i = 0; i < N; ++i) s.are[i] = U[C::i4 + i];
 #pragma unroll
-  for (int q = 0; q < 9; q++) s.A[q] = U[C::i5 + q];
-  float G[9], Gmag;
-  gmat_f(s.A, G, Gmag);
+  for (int q = 0; q < 9; q++) s.D[q] = U[C::i5 + q];
+  StrainF sE;
+  strain_f(s.D, sE);
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -150,7 +192,7 @@ __device__ void make_sol_f(const M5Consts &k, const float *U, float phi0, SolF<N
     const float press = U[RL::P + i];
     s.p[i] = press;
     c2 += (s.avf[i] * ir) * k.gamma_f[i] * (press + k.pinf_f[i]);
-    eos_stress_f(s.st, s.avf[i], press, G, Gmag, k.mu_f[i], nullptr);
+    eos_stress_f(s.st, s.avf[i], press, sE, k.mu_f[i], nullptr);
   }
   s.c2 = c2;
 }
@@ -209,7 +251,7 @@ __device__ __forceinline__ void ghost_f(const SolF<N> &L, int bc, SolF<N> &R) {
 
 template <int N>
 struct NCf {
-  float unc[3], avf[N], are[N], A[9];
+  float unc[3], avf[N], are[N], A[9];  // A itself (advected), not its deviation
 };
 
 // m5_star_region.c:3-158 in FP32.  dU receives the jump U*_K - U_K of the conservative
@@ -256,28 +298,28 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
              s13_S * w_S) / (r_S * (u_S - SK))
           : (re * (uK - SK) + s11K * uK - s12K * vK - s13K * wK + s11_S * u_S + s12_S * v_S +
              s13_S * w_S) / (r_S * (u_S + SK));
-  float Am[3][3], Al[3][3], AS[3][3], Ag[3][3];
+  // the star deformation, row 0 in the face frame
+  //   A*_0j = (A_0j (uK - SK) - A_1j (vK - v*) + A_2j (wK - w*)) / (u* - SK),
+  // rows 1 and 2 unchanged; on D = A - I the identity's share of row 0 is the jump
+  // (uK - u*) / (u* - SK), formed as that difference
+  float Dm[3][3], Dl[3][3], DS[3][3], Dg[3][3];
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) Am[i][j] = s.A[3 * i + j];
-  tens_to_local<F>(Am, Al);
+    for (int j = 0; j < 3; j++) Dm[i][j] = s.D[3 * i + j];
+  tens_to_local<F>(Dm, Dl);
   const float ius = 1.0f / (u_S - SK);
 #pragma unroll
   for (int j = 0; j < 3; j++) {
-    AS[0][j] = (Al[0][j] * (uK - SK) - Al[1][j] * (vK - v_S) + Al[2][j] * (wK - w_S)) * ius;
-    AS[1][j] = Al[1][j];
-    AS[2][j] = Al[2][j];
+    DS[0][j] = ((j == 0 ? uK - u_S : 0.0f) + Dl[0][j] * (uK - SK) -
+                ((j == 1 ? 1.0f : 0.0f) + Dl[1][j]) * (vK - v_S) +
+                ((j == 2 ? 1.0f : 0.0f) + Dl[2][j]) * (wK - w_S)) * ius;
+    DS[1][j] = Dl[1][j];
+    DS[2][j] = Dl[2][j];
   }
-  tens_to_global<F>(AS, Ag);
-  float G[9];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      G[3 * i + j] = Ag[i][0] * Ag[j][0] + Ag[i][1] * Ag[j][1] + Ag[i][2] * Ag[j][2];
-  const float Gmag = G[0] * (G[4] * G[8] - G[5] * G[7]) - G[1] * (G[3] * G[8] - G[5] * G[6]) +
-                     G[2] * (G[3] * G[7] - G[4] * G[6]);
+  tens_to_global<F>(DS, Dg);
+  StrainF sE;
+  strain_f(&Dg[0][0], sE);
 #pragma unroll
   for (int v = 0; v < N; ++v) {
     const float rm = s.ra[v] / s.avf[v];
@@ -286,7 +328,7 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
     // the reference takes p_k = -p_hydro here (m5_star_region.c:122)
     const float p_S = (-s.p[v] + pi) * (((ga - 1.0f) * rm + (ga + 1.0f) * rm_S) /
                                        ((ga - 1.0f) * rm_S + (ga + 1.0f) * rm)) - pi;
-    const float ael = elastic_energy_f(G, Gmag, k.mu_f[v]);
+    const float ael = elastic_energy_f(sE, k.mu_f[v]);
     const float eel = ael / (s.avf[v] * rm_S);
     const float e_S = (p_S + ga * pi) / (rm_S * (ga + 1.0f)) + eel;
     nc.are[v] = ar_S[v] * e_S;
@@ -311,7 +353,7 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
-    for (int j = 0; j < 3; j++) nc.A[3 * i + j] = Ag[i][j];
+    for (int j = 0; j < 3; j++) nc.A[3 * i + j] = Dg[i][j] + (i == j ? 1.0f : 0.0f);
   unsigned st = 0;
 #pragma unroll
   for (int iv = 0; iv < C::NC; ++iv)
@@ -342,14 +384,14 @@ __device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, bool cons, NCf<N>
 #pragma unroll
     for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
 #pragma unroll
-    for (int q = 0; q < 9; q++) nc.A[q] = (gfm || cons) ? s.A[q] : -s.A[q];
+    for (int q = 0; q < 9; q++) nc.A[q] = (gfm || cons) ? full_of(s.D, q) : -full_of(s.D, q);
   } else if (flag == 4) {  // symmetry face (m5_flux.c:58-66): the velocity is the caller's
 #pragma unroll
     for (int v = 0; v < N - 1; ++v) nc.avf[v] = s.avf[v];
 #pragma unroll
     for (int v = 0; v < N; ++v) nc.are[v] = s.are[v];
 #pragma unroll
-    for (int q = 0; q < 9; q++) nc.A[q] = s.A[q];
+    for (int q = 0; q < 9; q++) nc.A[q] = full_of(s.D, q);
   }
   const float ua = nc.unc[a];
 #pragma unroll
@@ -448,8 +490,9 @@ __device__ void symmetry_acc_f(const SolF<N> &Lc, bool cons, float Area, float *
   for (int d = 0; d < 3; d++) unc[d] = nc.unc[d];
 }
 
-// face record of a state V (FP64): conserved variables, the volume fractions as the FP64
-// form's make_sol clamps them, and each material's pressure recovered in FP64
+// face record of a state V (FP64): conserved variables (the deformation as D = A - I), the
+// volume fractions as the FP64 form's make_sol clamps them, and each material's pressure
+// recovered in FP64
 template <int N>
 __device__ void write_record(const M5Consts &k, const double *V, const double *press, float *out,
                              int64_t stride) {
@@ -472,7 +515,9 @@ __device__ void write_record(const M5Consts &k, const double *V, const double *p
   }
   at[N - 1] = 1.0 - sum;
 #pragma unroll
-  for (int i = 0; i < C::NEQ; i++) out[i * stride] = (float)V[i];
+  for (int i = 0; i < C::i5; i++) out[i * stride] = (float)V[i];
+#pragma unroll
+  for (int q = 0; q < 9; q++) out[(C::i5 + q) * stride] = dev_of(V + C::i5, q);
 #pragma unroll
   for (int i = 0; i < N - 1; ++i) out[(C::i3 + i) * stride] = (float)at[i];
   out[RL::AL * stride] = (float)at[N - 1];
@@ -480,13 +525,14 @@ __device__ void write_record(const M5Consts &k, const double *V, const double *p
 #pragma unroll
     for (int i = 0; i < N; ++i) out[(RL::P + i) * stride] = (float)press[i];
   } else {
-    float A[9], G[9], Gmag;
+    float D[9];
 #pragma unroll
-    for (int q = 0; q < 9; q++) A[q] = (float)V[C::i5 + q];
-    gmat_f(A, G, Gmag);
+    for (int q = 0; q < 9; q++) D[q] = dev_of(V + C::i5, q);
+    StrainF sE;
+    strain_f(D, sE);
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      const double ael = (double)elastic_energy_f(G, Gmag, k.mu_f[i]);
+      const double ael = (double)elastic_energy_f(sE, k.mu_f[i]);
       const double p = ((k.gamma[i] - 1.0) * (V[C::i4 + i] - ael) / at[i]) - k.gamma[i] * k.pinf[i];
       out[(RL::P + i) * stride] = (float)p;
     }
@@ -645,8 +691,8 @@ __device__ __forceinline__ void vf_limit_relax_df(const M5Consts &k, df *avf, bo
   avf[N - 1] = df_sub(df_make(1.0f), sum);
 }
 
-// m5_relaxationvec.c on a face state: FP32 partial densities, momentum and deformation in
-// v, the critical slots in cr as double-float pairs; the pressure recovery and the
+// m5_relaxationvec.c on a face state: FP32 partial densities, momentum and deformation
+// deviation D = A - I in v, the critical slots in cr as double-float pairs; the pressure recovery and the
 // energy-consistent equilibrium in double-float, the Newton iteration in FP32 (below).
 // PRELAX 1 (the two-material closed form) converts to FP64 and back.
 template <int N>
@@ -670,10 +716,12 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
   vf_limit_relax_df<N>(k, avf, true);
 #pragma unroll
   for (int iv = 0; iv < N; ++iv) avf0[iv] = avf[iv];
-  float G[9], Gmag;
-  gmat_f(v + C::i5, G, Gmag);
+  {
+    StrainF sE;
+    strain_f(v + C::i5, sE);
 #pragma unroll
-  for (int iv = 0; iv < N; ++iv) ael[iv] = elastic_energy_f(G, Gmag, k.mu_f[iv]);
+    for (int iv = 0; iv < N; ++iv) ael[iv] = elastic_energy_f(sE, k.mu_f[iv]);
+  }
   unsigned st = 0;
   df ratio = df_make(1.0f);
   if (N == 2 && k.prelax == 1) {  // closed form for two materials (only), in FP64
@@ -820,9 +868,10 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
     if (df_isnan(a2)) st |= FFV_ST_NAN;
     cr[N - 1 + iv] = a2;
   }
-  const float rf32 = df_to_float(ratio);
+  // A <- ratio A, i.e. D <- ratio D + (ratio - 1) I
+  const float rf32 = df_to_float(ratio), rm1 = df_to_float(df_add_f(ratio, -1.0f));
 #pragma unroll
-  for (int q = 0; q < 9; ++q) v[C::i5 + q] *= rf32;
+  for (int q = 0; q < 9; ++q) v[C::i5 + q] = rf32 * v[C::i5 + q] + ((q == 0 || q == 4 || q == 8) ? rm1 : 0.0f);
   p_out = df_to_float(p);
   if (ratio_out) *ratio_out = ratio;
   return st;
@@ -835,11 +884,13 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
 template <int N>
 __device__ unsigned relax_cell_df(const M5Consts &k, double *V) {
   using C = K5<N>;
-  // relax_face_df's inputs: the FP32 partial densities, momentum and deformation, and the
-  // critical slots as pairs
+  // relax_face_df's inputs: the FP32 partial densities, momentum and deformation deviation,
+  // and the critical slots as pairs
   float v[C::NEQ];
 #pragma unroll
-  for (int i = 0; i < C::NEQ; i++) v[i] = (float)V[i];
+  for (int i = 0; i < C::i5; i++) v[i] = (float)V[i];
+#pragma unroll
+  for (int q = 0; q < 9; q++) v[C::i5 + q] = dev_of(V + C::i5, q);
   df cr[2 * N];
 #pragma unroll
   for (int j = 0; j < 2 * N; j++) cr[j] = df_from_double(V[crit_slot<N>(j)]);
@@ -861,8 +912,9 @@ __device__ unsigned relax_cell_df(const M5Consts &k, double *V) {
 }
 
 // ------------------------------------------------------------------------------ kernels
-// FP32 copy of the state for the reconstruction (made once per cell per stage), and the
-// low parts of the critical slots' double-float pairs: Sflo[j][c] = S - (double)(float)S
+// FP32 copy of the state for the reconstruction (made once per cell per stage) -- the
+// deformation as its deviation D = A - I -- and the low parts of the critical slots'
+// double-float pairs: Sflo[j][c] = S - (double)(float)S
 template <int N>
 __global__ void __launch_bounds__(256) m5f_shadow(int64_t n, const double *__restrict__ S,
                                                   float *__restrict__ Sf, float *__restrict__ Sflo) {
@@ -871,7 +923,8 @@ __global__ void __launch_bounds__(256) m5f_shadow(int64_t n, const double *__res
        c += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int v = 0; v < C::NEQ; v++) {
-      const double x = S[(int64_t)v * n + c];
+      const double x = S[(int64_t)v * n + c] -
+                       ((v == C::i5 || v == C::i5 + 4 || v == C::i5 + 8) ? 1.0 : 0.0);
       const float h = (float)x;
       Sf[(int64_t)v * n + c] = h;
 #pragma unroll
@@ -1175,10 +1228,14 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
     sum = hi;
   }
   at[N - 1] = 1.0 - sum;
-  float A[9], G[9], Gmag, avf[N], ast[N][3][3], st_all[3][3];
+  float A[9], D[9], avf[N], ast[N][3][3], st_all[3][3];
 #pragma unroll
-  for (int q = 0; q < 9; q++) A[q] = (float)s[C::i5 + q];
-  gmat_f(A, G, Gmag);
+  for (int q = 0; q < 9; q++) {
+    D[q] = dev_of(s + C::i5, q);
+    A[q] = (float)s[C::i5 + q];
+  }
+  StrainF sE;
+  strain_f(D, sE);
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -1186,12 +1243,12 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
 #pragma unroll
   for (int i = 0; i < N; ++i) {
     // the material pressure only enters the FP32 stress: recovered in double-float
-    const float ael = elastic_energy_f(G, Gmag, k.mu_f[i]);
+    const float ael = elastic_energy_f(sE, k.mu_f[i]);
     const df a_d = df_from_double(at[i]);
     const df p = df_sub(df_div(df_mul(k.gm1_d[i], df_add_f(df_from_double(s[C::i4 + i]), -ael)), a_d),
                         k.gpi_d[i]);
     avf[i] = a_d.hi;
-    eos_stress_f(st_all, avf[i], df_to_float(p), G, Gmag, k.mu_f[i], ast[i]);
+    eos_stress_f(st_all, avf[i], df_to_float(p), sE, k.mu_f[i], ast[i]);
   }
   double rhs[NA];
   float rhsA[9], nc[N - 1 + N + 9];
@@ -1352,15 +1409,17 @@ __global__ void __launch_bounds__(128) m5f_indicator_fields(int64_t n, M5Consts 
 #pragma unroll
   for (int i = 0; i < N - 1; ++i) sum = df_add(sum, at[i]);
   at[N - 1] = df_sub(df_make(1.0f), sum);
-  float A[9], G[9], Gmag;
+  float D[9];
 #pragma unroll
-  for (int q = 0; q < 9; q++) A[q] = (float)S[(int64_t)(C::i5 + q) * n + c];
-  gmat_f(A, G, Gmag);
+  for (int q = 0; q < 9; q++)
+    D[q] = (float)(S[(int64_t)(C::i5 + q) * n + c] - ((q == 0 || q == 4 || q == 8) ? 1.0 : 0.0));
+  StrainF sE;
+  strain_f(D, sE);
   float st[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
   df p = df_make(0.0f);
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    const float ael = elastic_energy_f(G, Gmag, k.mu_f[i]);
+    const float ael = elastic_energy_f(sE, k.mu_f[i]);
     const df pk = df_sub(df_div(df_mul(k.gm1_d[i], df_add_f(df_from_double(S[(int64_t)(C::i4 + i) * n + c]), -ael)),
                                 at[i]),
                          k.gpi_d[i]);
@@ -1368,7 +1427,7 @@ __global__ void __launch_bounds__(128) m5f_indicator_fields(int64_t n, M5Consts 
     // the von Mises stress depends on the deviator only, to which -alpha_k p_k I adds
     // nothing: the elastic part alone (in FP32 the isotropic terms, up to ~1e10 for a nearly
     // absent material, would round away the deviator)
-    eos_stress_f(st, 0.0f, 0.0f, G, Gmag, k.mu_f[i], nullptr);
+    eos_stress_f(st, 0.0f, 0.0f, sE, k.mu_f[i], nullptr);
   }
   const float tr = (st[0][0] + st[1][1] + st[2][2]) * (1.0f / 3.0f);
   float j2 = 0.0f;
