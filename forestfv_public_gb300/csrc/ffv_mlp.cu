@@ -8,10 +8,13 @@
 // 144 with zeros.  Output: the probability that the plain criterion will ask for a finer
 // level within the prediction horizon.
 //
-// Arithmetic: BF16 operands, FP32 accumulation, on the tensor cores with warp-level
-// mma.sync m16n8k16 (16 samples per warp).  The backward pass recomputes the forward pass
-// of its tile, forms the weight gradients as (16-sample) tensor-core products into
-// shared-memory FP32 accumulators and adds them to the global gradient once per block.
+// Arithmetic: BF16 operands, FP32 accumulation on the tensor cores.  Inference (features,
+// both layers and the marks in one kernel, mlp_infer_tc): a CTA builds the feature rows of
+// 128 cells in shared memory and one thread issues tcgen05.mma (M = 128, N = 64) for each
+// layer, the accumulators in tensor memory.  Training: warp-level mma.sync m16n8k16
+// (16 samples per warp); the backward pass recomputes the forward pass of its tile, forms
+// the weight gradients as (16-sample) tensor-core products into shared-memory FP32
+// accumulators and adds them to the global gradient once per block.
 // Where a tensor-core product needs an operand the forward pass holds in FP32 (the hidden
 // activations, the pre-activation gradients) it is rounded to BF16; the CPU restatement
 // (oracle/mlp.py) rounds at the same points.
@@ -23,6 +26,7 @@
 #include "ffv.h"
 #include "ffv_device.cuh"
 #include "ffv_m5.cuh"
+#include "ffv_tc.cuh"
 
 namespace {
 
@@ -57,12 +61,65 @@ __device__ __forceinline__ float gelu_grad(float x) {
 }
 
 // ------------------------------------------------------------------------- features
-__device__ __forceinline__ int64_t face_step(const ffv_dmesh &m, int64_t c, int f) {
-  const uint32_t kind = ffv_face_kind(m.info[c], f);
-  if (kind & FFV_FK_BC) return c;
-  const int32_t s = m.nbr[(int64_t)f * m.n + c];
-  if (kind == FFV_FK_FINER) return m.sub[4 * (int64_t)s];
-  return s;
+// the cells across faces fneg and fpos of cell e: a boundary face keeps the cell, a face
+// with four finer neighbours takes the first of them
+__device__ __forceinline__ void face_steps(const ffv_dmesh &m, int32_t e, int fneg, int fpos,
+                                           int32_t &en, int32_t &ep) {
+  const uint32_t info = m.info[e];
+  const uint32_t kn = ffv_face_kind(info, fneg), kp = ffv_face_kind(info, fpos);
+  en = e;
+  ep = e;
+  if (!(kn & FFV_FK_BC)) {
+    const int32_t s = m.nbr[(int64_t)fneg * m.n + e];
+    en = kn == FFV_FK_FINER ? m.sub[4 * (int64_t)s] : s;
+  }
+  if (!(kp & FFV_FK_BC)) {
+    const int32_t s = m.nbr[(int64_t)fpos * m.n + e];
+    ep = kp == FFV_FK_FINER ? m.sub[4 * (int64_t)s] : s;
+  }
+}
+
+// the 27 stencil cells of c, o = (dx + 1) + 3 (dy + 1) + 9 (dz + 1): the step along x, then
+// along y, then along z.  The walks share their prefixes: 2 + 6 + 18 independent face steps
+// in three dependent rounds.
+__device__ __forceinline__ void stencil27(const ffv_dmesh &m, int32_t c, int32_t e[27]) {
+  int32_t x[3], y[9];
+  x[1] = c;
+  face_steps(m, c, 0, 2, x[0], x[2]);
+#pragma unroll
+  for (int ix = 0; ix < 3; ix++) {
+    y[ix + 3] = x[ix];
+    face_steps(m, x[ix], 3, 1, y[ix], y[ix + 6]);
+  }
+#pragma unroll
+  for (int j = 0; j < 9; j++) {
+    e[j + 9] = y[j];
+    face_steps(m, y[j], 4, 5, e[j], e[j + 18]);
+  }
+}
+
+// the 135 normalised features of a cell as BF16, eight per 16-byte chunk (chunk 16 holds
+// features 128-134 and a zero, chunk 17 zeros), handed to put(chunk, uint4)
+template <typename Put>
+__device__ __forceinline__ void cell_features(const ffv_dmesh &m, const float *__restrict__ F,
+                                              const float mean[5], const float istd[5], int32_t c,
+                                              Put put) {
+  int32_t e[27];
+  stencil27(m, c, e);
+  uint32_t w[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+  for (int o = 0; o < 27; o++)
+#pragma unroll
+    for (int q = 0; q < 5; q++) {
+      const int k = 5 * o + q;
+      const bf16 v = __float2bfloat16_rn((F[(int64_t)q * m.n + e[o]] - mean[q]) * istd[q]);
+      const uint32_t u = __bfloat16_as_ushort(v);
+      if ((k & 1) == 0) w[(k & 7) >> 1] = u;
+      else w[(k & 7) >> 1] |= u << 16;
+      if ((k & 7) == 7) put(k >> 3, make_uint4(w[0], w[1], w[2], w[3]));
+    }
+  put(NIN >> 3, make_uint4(w[0], w[1], w[2], w[3] & 0xFFFFu));
+  put(KIN / 8 - 1, make_uint4(0u, 0u, 0u, 0u));
 }
 
 // A block builds its 128 feature rows in shared memory (row stride 146 BF16 = 73 words,
@@ -84,26 +141,12 @@ __global__ void __launch_bounds__(GATHER_TPB) mlp_gather(ffv_dmesh m, const floa
       istd[q] = 1.0f / norm[5 + q];
     }
     uint32_t *row = tile + threadIdx.x * GATHER_SW;
-    bf16 carry = __float2bfloat16_rn(0.0f);
-    int k = 0;  // feature index
-#pragma unroll 1
-    for (int o = 0; o < 27; o++) {
-      const int dx = o % 3 - 1, dy = (o / 3) % 3 - 1, dz = o / 9 - 1;
-      int64_t e = c;
-      if (dx) e = face_step(m, e, dx < 0 ? 0 : 2);
-      if (dy) e = face_step(m, e, dy < 0 ? 3 : 1);
-      if (dz) e = face_step(m, e, dz < 0 ? 4 : 5);
-#pragma unroll
-      for (int q = 0; q < 5; q++, k++) {
-        const bf16 v = __float2bfloat16_rn((F[(int64_t)q * m.n + e] - mean[q]) * istd[q]);
-        if (k & 1) row[k >> 1] = pack2(carry, v);
-        else carry = v;
-      }
-    }
-    // k == 135: the last feature and the zero padding up to 144
-    row[NIN >> 1] = pack2(carry, __float2bfloat16_rn(0.0f));
-#pragma unroll
-    for (int w = (NIN >> 1) + 1; w < KIN / 2; w++) row[w] = 0u;
+    cell_features(m, F, mean, istd, (int32_t)c, [&](int ch, uint4 v) {
+      row[4 * ch] = v.x;
+      row[4 * ch + 1] = v.y;
+      row[4 * ch + 2] = v.z;
+      row[4 * ch + 3] = v.w;
+    });
   }
   __syncthreads();
   const int64_t rows = m.n - c0 < GATHER_TPB ? m.n - c0 : GATHER_TPB;
@@ -263,31 +306,162 @@ constexpr size_t smem_bytes(bool train) {
 // FP32 gradient accumulators of a training block, after the operand area
 constexpr size_t ACC_FLOATS = NH * KIN + NH * NH + 3 * NH + 1 + 1;  // ... + b3 + loss
 
-__global__ void __launch_bounds__(TPB) mlp_forward_kernel(const bf16 *__restrict__ X, int64_t n,
-                                                          const bf16 *__restrict__ W1,
-                                                          const bf16 *__restrict__ W2,
-                                                          const float *__restrict__ P,
-                                                          float *__restrict__ prob) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const Smem s = carve(smem, false);
-  stage_weights(s, W1, W2, nullptr, P, false);
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, q = lane & 3;
-  bf16 *Xs = s.X + warp * 16 * SX, *H1s = s.H1 + warp * 16 * SH;
-  const float b3 = P[OFF_B3];
-  const int64_t ntiles = (n + 15) / 16;
-  for (int64_t t = (int64_t)blockIdx.x * WARPS + warp; t < ntiles; t += (int64_t)gridDim.x * WARPS) {
-    const int64_t r0 = t * 16;
-    const int valid = (int)((n - r0) < 16 ? (n - r0) : 16);
-    load_tile(Xs, X, valid, [&](int r) { return r0 + r; });
-    float a1[8][4], a2[8][4], zg, zg8;
-    tile_forward(s, Xs, H1s, a1, a2, zg, zg8);
-    if (q == 0) {
-      if (g < valid) prob[r0 + g] = 1.0f / (1.0f + expf(-(zg + b3)));
-      if (g + 8 < valid) prob[r0 + g + 8] = 1.0f / (1.0f + expf(-(zg8 + b3)));
-    }
-    __syncwarp();
+// ------------------------------------------------------------------ inference (tcgen05)
+// One CTA of 128 threads per 128-cell tile (persistent over tiles), thread r owning cell
+// row r.  Shared memory, canonical K-major BF16 tiles (ffv_tc.cuh): the feature tile X
+// [128][144] (later the first hidden layer H [128][64] over it), W1 [64][144], W2 [64][64],
+// then b1, b2, w3 in FP32.  Tensor memory: 64 FP32 columns x 128 lanes, the accumulator of
+// either layer (lane r = row r).  Per tile: rows built (stencil gather or copied feature
+// rows) -> 9 MMAs (K = 16) of layer 1 -> GELU + BF16 of row r into H -> 4 MMAs of layer 2 ->
+// GELU, the w3 dot product and the sigmoid of row r.  The MMAs take ~1 us of a tile's time:
+// the gather dominates, and three CTAs per SM overlap one another's phases.
+constexpr int TC_ROWS = 128;
+constexpr int TC_SBO_X = (KIN / 8) * 128, TC_SBO_H = (NH / 8) * 128;
+constexpr int TC_W1 = TC_ROWS * KIN * 2;     // byte offsets in the dynamic shared memory
+constexpr int TC_W2 = TC_W1 + NH * KIN * 2;
+constexpr int TC_VEC = TC_W2 + NH * NH * 2;
+constexpr int TC_SMEM = TC_VEC + 3 * NH * 4;
+constexpr int TC_CTAS_PER_SM = 3;
+constexpr int TC_TMEM_COLS = 64;
+constexpr int TC_WAIT_POLLS = 1 << 22;  // an MMA group takes ~1 us; this is far beyond it
+static_assert(TC_SMEM * TC_CTAS_PER_SM <= 227 * 1024, "shared memory of three CTAs per SM");
+static_assert(TC_TMEM_COLS * TC_CTAS_PER_SM <= 512, "tensor memory of three CTAs per SM");
+
+template <bool GATHER>
+__global__ void __launch_bounds__(TC_ROWS, TC_CTAS_PER_SM)
+    mlp_infer_tc(ffv_dmesh m, const float *__restrict__ F, const float *__restrict__ norm,
+                 const bf16 *__restrict__ X, int64_t n, const bf16 *__restrict__ W1,
+                 const bf16 *__restrict__ W2, const float *__restrict__ P, float *__restrict__ prob,
+                 uint8_t *__restrict__ marks, float threshold, int accumulate,
+                 unsigned *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint32_t tmem_holder;
+  __shared__ __align__(8) uint64_t bar;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  for (int i = tid; i < NH * (KIN / 8); i += TC_ROWS) {
+    const int r = i / (KIN / 8), ch = i % (KIN / 8);
+    *reinterpret_cast<uint4 *>(sm + TC_W1 + tc::kmajor_offset(r, 8 * ch, KIN)) =
+        *reinterpret_cast<const uint4 *>(W1 + r * KIN + 8 * ch);
   }
+  for (int i = tid; i < NH * (NH / 8); i += TC_ROWS) {
+    const int r = i / (NH / 8), ch = i % (NH / 8);
+    *reinterpret_cast<uint4 *>(sm + TC_W2 + tc::kmajor_offset(r, 8 * ch, NH)) =
+        *reinterpret_cast<const uint4 *>(W2 + r * NH + 8 * ch);
+  }
+  float *b1s = reinterpret_cast<float *>(sm + TC_VEC), *b2s = b1s + NH, *w3s = b2s + NH;
+  for (int i = tid; i < NH; i += TC_ROWS) {
+    b1s[i] = P[OFF_B1 + i];
+    b2s[i] = P[OFF_B2 + i];
+    w3s[i] = P[OFF_W3 + i];
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_holder, TC_TMEM_COLS);
+  if (tid == 0) tc::mbar_init(&bar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = tmem_holder;
+  const uint32_t row_tmem = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
+  const uint32_t xs = tc::smem_addr(sm), w1s = tc::smem_addr(sm + TC_W1),
+                 w2s = tc::smem_addr(sm + TC_W2);
+  constexpr uint32_t idesc = tc::idesc_bf16_f32(TC_ROWS, NH);
+  const float b3 = P[OFF_B3];
+  float mean[5], istd[5];
+#pragma unroll
+  for (int q = 0; q < 5; q++) {
+    mean[q] = GATHER ? norm[q] : 0.0f;
+    istd[q] = GATHER ? 1.0f / norm[5 + q] : 1.0f;
+  }
+  const int64_t ntiles = (n + TC_ROWS - 1) / TC_ROWS;
+  int failed_parity = -1;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int64_t c = t * TC_ROWS + tid;
+    const bool valid = c < n;
+    auto put = [&](int ch, uint4 v) {
+      *reinterpret_cast<uint4 *>(sm + tc::kmajor_offset(tid, 8 * ch, KIN)) = v;
+    };
+    if (!valid) {
+#pragma unroll 1
+      for (int ch = 0; ch < KIN / 8; ch++) put(ch, make_uint4(0u, 0u, 0u, 0u));
+    } else if (GATHER) {
+      cell_features(m, F, mean, istd, (int32_t)c, put);
+    } else {
+#pragma unroll
+      for (int ch = 0; ch < KIN / 8; ch++) put(ch, *reinterpret_cast<const uint4 *>(X + c * KIN + 8 * ch));
+    }
+    // layer 1: pre-activations of the 128 rows into tensor memory
+    tc::fence_async_shared();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+#pragma unroll
+      for (int kk = 0; kk < KIN / 16; kk++)
+        tc::mma_bf16(tmem, tc::sdesc(xs + 256 * kk, 128, TC_SBO_X), tc::sdesc(w1s + 256 * kk, 128, TC_SBO_X),
+                     idesc, kk > 0);
+      tc::commit(&bar);
+    }
+    if (__syncthreads_or(!tc::mbar_wait(&bar, 0, TC_WAIT_POLLS))) {
+      failed_parity = 0;
+      break;
+    }
+    tc::fence_after_sync();
+#pragma unroll
+    for (int c0 = 0; c0 < NH; c0 += 16) {
+      float a[16];
+      tc::tmem_ld16(row_tmem + c0, a);
+      uint32_t pk[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        pk[j] = pack2(__float2bfloat16_rn(gelu(a[2 * j] + b1s[c0 + 2 * j])),
+                      __float2bfloat16_rn(gelu(a[2 * j + 1] + b1s[c0 + 2 * j + 1])));
+      *reinterpret_cast<uint4 *>(sm + tc::kmajor_offset(tid, c0, NH)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+      *reinterpret_cast<uint4 *>(sm + tc::kmajor_offset(tid, c0 + 8, NH)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+    }
+    // layer 2 over H (the feature tile's first 16 KB: layer 1 has finished reading it)
+    tc::fence_async_shared();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0) {
+#pragma unroll
+      for (int kk = 0; kk < NH / 16; kk++)
+        tc::mma_bf16(tmem, tc::sdesc(xs + 256 * kk, 128, TC_SBO_H), tc::sdesc(w2s + 256 * kk, 128, TC_SBO_H),
+                     idesc, kk > 0);
+      tc::commit(&bar);
+    }
+    if (__syncthreads_or(!tc::mbar_wait(&bar, 1, TC_WAIT_POLLS))) {
+      failed_parity = 1;
+      break;
+    }
+    tc::fence_after_sync();
+    float z = 0.0f;
+#pragma unroll
+    for (int c0 = 0; c0 < NH; c0 += 16) {
+      float a[16];
+      tc::tmem_ld16(row_tmem + c0, a);
+#pragma unroll
+      for (int j = 0; j < 16; j++) z += gelu(a[j] + b2s[c0 + j]) * w3s[c0 + j];
+    }
+    if (valid) {
+      const float p = 1.0f / (1.0f + expf(-(z + b3)));
+      if (prob) prob[c] = p;
+      if (marks) {
+        const uint8_t hit = p > threshold ? 1 : 0;
+        marks[c] = accumulate ? (uint8_t)(marks[c] | hit) : hit;
+      }
+    }
+    // the next tile's MMAs (after its barrier) overwrite the accumulator these loads read
+    tc::fence_before_sync();
+  }
+  if (failed_parity >= 0) {
+    // a wait ran out: report it, give the MMAs in flight one more bounded wait, free the
+    // tensor memory and leave (the tiles not finished keep their outputs)
+    if (tid == 0) atomicOr(err, 1u);
+    tc::mbar_wait(&bar, (uint32_t)failed_parity, TC_WAIT_POLLS);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, TC_TMEM_COLS);
 }
 
 // row index of sample i of a training step: identity (seed 0) or a hashed draw
@@ -478,16 +652,6 @@ __global__ void __launch_bounds__(TPB) mlp_train_kernel(const bf16 *__restrict__
 }
 
 // AdamW (decoupled weight decay on W1, W2, w3; none on the biases)
-// marks[c] = (accumulate ? marks[c] : 0) | (prob[c] > threshold)
-__global__ void mlp_mark(int64_t n, const float *__restrict__ prob, float threshold,
-                         uint8_t *__restrict__ marks, int accumulate) {
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    const uint8_t hit = prob[c] > threshold ? 1 : 0;
-    marks[c] = accumulate ? (uint8_t)(marks[c] | hit) : hit;
-  }
-}
-
 __global__ void mlp_adamw(float *__restrict__ P, const float *__restrict__ G, float *__restrict__ M,
                           float *__restrict__ V, float lr, float wd, float b1, float b2, float eps,
                           float c1, float c2) {
@@ -508,7 +672,7 @@ __global__ void mlp_adamw(float *__restrict__ P, const float *__restrict__ G, fl
 }  // namespace
 
 struct ffv_mlp {
-  int device;
+  int device, nsm;
   cudaStream_t stream;
   float *d_P, *d_G, *d_M, *d_V, *d_norm, *d_loss;
   bf16 *d_W1, *d_W2, *d_W2T;
@@ -516,7 +680,8 @@ struct ffv_mlp {
   // predict buffers
   int64_t cap;
   float *d_F, *d_prob;
-  bf16 *d_X;
+  // inference wait timeouts: mapped pinned word, set by the device, read by the host
+  unsigned *h_err, *d_err;
 };
 
 namespace {
@@ -536,27 +701,41 @@ int ensure_cap(ffv_mlp *m, int64_t n) {
   if (m->cap >= n) return FFV_OK;
   cudaFree(m->d_F);
   cudaFree(m->d_prob);
-  cudaFree(m->d_X);
   m->d_F = m->d_prob = nullptr;
-  m->d_X = nullptr;
   m->cap = 0;
   if (cudaMalloc(&m->d_F, sizeof(float) * 5 * n) != cudaSuccess ||
-      cudaMalloc(&m->d_prob, sizeof(float) * n) != cudaSuccess ||
-      cudaMalloc(&m->d_X, sizeof(bf16) * KIN * n) != cudaSuccess)
+      cudaMalloc(&m->d_prob, sizeof(float) * n) != cudaSuccess)
     return FFV_ERR_NOMEM;
   m->cap = n;
   return FFV_OK;
 }
 
-int forward(ffv_mlp *m, const bf16 *X, int64_t n, float *prob, cudaStream_t st) {
-  const size_t sb = smem_bytes(false);
-  MCK(cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-  const int64_t tiles = (n + 15) / 16;
-  int64_t blocks = (tiles + WARPS - 1) / WARPS;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  if (blocks < 1) blocks = 1;
-  mlp_forward_kernel<<<(unsigned)blocks, TPB, sb, st>>>(X, n, m->d_W1, m->d_W2, m->d_P, prob);
+// the fused inference kernel over n rows: feature rows X (dm unused), or the stencil gather
+// of the fields F on mesh dm (X unused); probabilities and/or marks out
+int infer(ffv_mlp *m, bool gather, const ffv_dmesh &dm, const float *F, const bf16 *X, int64_t n,
+          float *prob, uint8_t *marks, float threshold, int accumulate, cudaStream_t st) {
+  if (n <= 0) return FFV_OK;
+  const int64_t tiles = (n + TC_ROWS - 1) / TC_ROWS;
+  int64_t blocks = (int64_t)m->nsm * TC_CTAS_PER_SM;
+  if (blocks > tiles) blocks = tiles;
+  if (gather) {
+    MCK(cudaFuncSetAttribute(mlp_infer_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    mlp_infer_tc<true><<<(unsigned)blocks, TC_ROWS, TC_SMEM, st>>>(
+        dm, F, m->d_norm, nullptr, n, m->d_W1, m->d_W2, m->d_P, prob, marks, threshold, accumulate, m->d_err);
+  } else {
+    MCK(cudaFuncSetAttribute(mlp_infer_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+    mlp_infer_tc<false><<<(unsigned)blocks, TC_ROWS, TC_SMEM, st>>>(
+        dm, nullptr, nullptr, X, n, m->d_W1, m->d_W2, m->d_P, prob, marks, threshold, accumulate, m->d_err);
+  }
   return mlp_cuda(cudaGetLastError());
+}
+
+// a timeout recorded by an inference kernel that has finished (the word is cleared)
+int take_timeout(ffv_mlp *m) {
+  const unsigned e = *(volatile unsigned *)m->h_err;
+  if (!e) return FFV_OK;
+  *(volatile unsigned *)m->h_err = 0u;
+  return FFV_ERR_TIMEOUT;
 }
 
 int grad(ffv_mlp *m, const bf16 *X, const float *y, int64_t N, int64_t B, uint64_t seed,
@@ -625,6 +804,9 @@ int ffv_mlp_create(ffv_mlp **out, int device, uint64_t seed) {
   ffv_mlp *m = (ffv_mlp *)calloc(1, sizeof(ffv_mlp));
   if (!m) return FFV_ERR_NOMEM;
   m->device = device;
+  if (cudaDeviceGetAttribute(&m->nsm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      m->nsm < 1)
+    m->nsm = 1;
   float *h = (float *)malloc(sizeof(float) * NPARAM);
   const float norm[10] = {0, 0, 0, 0, 0, 1, 1, 1, 1, 1};
   int rc = FFV_OK;
@@ -637,9 +819,12 @@ int ffv_mlp_create(ffv_mlp **out, int device, uint64_t seed) {
       cudaMalloc(&m->d_loss, sizeof(float)) != cudaSuccess ||
       cudaMalloc(&m->d_W1, sizeof(bf16) * NH * KIN) != cudaSuccess ||
       cudaMalloc(&m->d_W2, sizeof(bf16) * NH * NH) != cudaSuccess ||
-      cudaMalloc(&m->d_W2T, sizeof(bf16) * NH * NH) != cudaSuccess) {
-    rc = h ? FFV_ERR_NOMEM : FFV_ERR_NOMEM;
+      cudaMalloc(&m->d_W2T, sizeof(bf16) * NH * NH) != cudaSuccess ||
+      cudaHostAlloc(&m->h_err, sizeof(unsigned), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer(&m->d_err, m->h_err, 0) != cudaSuccess) {
+    rc = FFV_ERR_NOMEM;
   }
+  if (rc == FFV_OK) *m->h_err = 0u;
   if (rc == FFV_OK) {
     init_params(h, seed);
     if (cudaMemcpy(m->d_P, h, sizeof(float) * NPARAM, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -674,7 +859,7 @@ int ffv_mlp_destroy(ffv_mlp *m) {
   cudaFree(m->d_W2T);
   cudaFree(m->d_F);
   cudaFree(m->d_prob);
-  cudaFree(m->d_X);
+  cudaFreeHost(m->h_err);
   if (m->stream) cudaStreamDestroy(m->stream);
   free(m);
   return FFV_OK;
@@ -748,10 +933,11 @@ int ffv_mlp_forward(ffv_mlp *m, const void *X_dev, int64_t n, float *prob_dev) {
   if (!m || !X_dev || !prob_dev || n < 0) return FFV_ERR_ARG;
   MCK(cudaSetDevice(m->device));
   if (n == 0) return FFV_OK;
-  int rc = forward(m, (const bf16 *)X_dev, n, prob_dev, m->stream);
+  int rc = infer(m, false, ffv_dmesh{}, nullptr, (const bf16 *)X_dev, n, prob_dev, nullptr, 0.0f, 0,
+                 m->stream);
   if (rc != FFV_OK) return rc;
   MCK(cudaStreamSynchronize(m->stream));
-  return FFV_OK;
+  return take_timeout(m);
 }
 
 int ffv_mlp_predict(ffv_ctx *ctx, ffv_mlp *m, float *prob_host) {
@@ -764,13 +950,11 @@ int ffv_mlp_predict(ffv_ctx *ctx, ffv_mlp *m, float *prob_host) {
   rc = ensure_cap(m, v.dm.n);
   if (rc != FFV_OK) return rc;
   launch_fields(v, m->d_F);
-  mlp_gather<<<(unsigned)((v.dm.n + 127) / 128), 128, 0, v.st>>>(v.dm, m->d_F, m->d_norm, m->d_X);
-  MCK(cudaGetLastError());
-  rc = forward(m, m->d_X, v.dm.n, m->d_prob, v.st);
+  rc = infer(m, true, v.dm, m->d_F, nullptr, v.dm.n, m->d_prob, nullptr, 0.0f, 0, v.st);
   if (rc != FFV_OK) return rc;
   MCK(cudaMemcpyAsync(prob_host, m->d_prob, sizeof(float) * v.dm.n, cudaMemcpyDeviceToHost, v.st));
   MCK(cudaStreamSynchronize(v.st));
-  return FFV_OK;
+  return take_timeout(m);
 }
 
 int ffv_mlp_mark(ffv_ctx *ctx, ffv_mlp *m, float threshold, uint8_t *marks_dev,
@@ -783,14 +967,11 @@ int ffv_mlp_mark(ffv_ctx *ctx, ffv_mlp *m, float threshold, uint8_t *marks_dev,
   MCK(cudaSetDevice(v.device));
   rc = ensure_cap(m, v.dm.n);
   if (rc != FFV_OK) return rc;
-  launch_fields(v, m->d_F);
-  mlp_gather<<<(unsigned)((v.dm.n + 127) / 128), 128, 0, v.st>>>(v.dm, m->d_F, m->d_norm, m->d_X);
-  MCK(cudaGetLastError());
-  rc = forward(m, m->d_X, v.dm.n, m->d_prob, v.st);
+  // a timeout of an earlier call (this call is not waited for)
+  rc = take_timeout(m);
   if (rc != FFV_OK) return rc;
-  mlp_mark<<<152 * 4, 256, 0, v.st>>>(v.dm.n, m->d_prob, threshold, marks_dev, accumulate);
-  MCK(cudaGetLastError());
-  return FFV_OK;
+  launch_fields(v, m->d_F);
+  return infer(m, true, v.dm, m->d_F, nullptr, v.dm.n, nullptr, marks_dev, threshold, accumulate, v.st);
 }
 
 int ffv_mlp_grad(ffv_mlp *m, const void *X_dev, const float *y_dev, int64_t B, float *grad_host,

@@ -320,7 +320,10 @@ int ffv_mlp_set_norm(ffv_mlp *mlp, const float *mean, const float *stdev);
 int ffv_mlp_fields(ffv_ctx *ctx, float *F_dev);
 /* feature rows of the context's state into X_dev (device, BF16 [n][144]) */
 int ffv_mlp_features(ffv_ctx *ctx, ffv_mlp *mlp, void *X_dev);
-/* probabilities of n feature rows (device pointers) */
+/* probabilities of n feature rows (device pointers).  Inference runs on the fifth-generation
+ * tensor cores (tcgen05.mma, accumulators in tensor memory) with bounded waits: a wait that
+ * runs out is returned as FFV_ERR_TIMEOUT (by ffv_mlp_forward and ffv_mlp_predict, which
+ * wait for the device; by the next ffv_mlp_mark, which does not). */
 int ffv_mlp_forward(ffv_mlp *mlp, const void *X_dev, int64_t n, float *prob_dev);
 /* features + forward of the context's state, probabilities to the host (n) */
 int ffv_mlp_predict(ffv_ctx *ctx, ffv_mlp *mlp, float *prob_host);

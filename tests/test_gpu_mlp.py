@@ -52,6 +52,41 @@ def test_forward_matches_oracle(built_lib):
     ind.close()
 
 
+def test_forward_many_tiles_matches_oracle(built_lib):
+    """More 128-row tiles than the inference kernel has CTAs (each CTA loops over several),
+    the last tile partial."""
+    rng = np.random.default_rng(4)
+    ind = Indicator(seed=3)
+    P = random_params(rng)
+    ind.set_params(P)
+    Xf, X, _, _ = data(rng, 200_003)
+    p = ind.forward(X).cpu().numpy()
+    ref, _ = mlp.forward(P.astype(np.float64), Xf)
+    assert np.abs(p - ref).max() < 2e-3 and np.abs(p - ref).mean() < 1e-4
+    ind.close()
+
+
+def test_predict_equals_forward_of_features(built_lib):
+    """ffv_mlp_predict (stencil gather fused with the network) gives the bits of
+    ffv_mlp_forward on the rows of ffv_mlp_features."""
+    g = load_golden("m5_wall_amr")
+    m = mesh_from_golden(g)
+    q = m5_params(g)
+    s = Solver(model=5, gamma=q["gamma"], pinf=q["pinf"], mu=q["mu"], amin=q["amin"],
+               avf_lim=q["avf_lim"], prelax=q["prelax"])
+    s.set_mesh(m)
+    s.upload_state(np.ascontiguousarray(g["S_final"].T))
+    ind = Indicator(seed=5)
+    ind.set_params(random_params(np.random.default_rng(11)))
+    F = ind.fields(s).cpu().numpy().astype(np.float64)
+    ind.set_norm(F.mean(axis=1), F.std(axis=1) + 1e-3)
+    p = ind.predict(s)
+    pf = ind.forward(ind.features(s)).cpu().numpy()
+    assert np.array_equal(p, pf)
+    ind.close()
+    s.close()
+
+
 @pytest.mark.parametrize("B", [16, 1000, 8192])
 def test_gradient_matches_oracle(B, built_lib):
     rng = np.random.default_rng(B)
