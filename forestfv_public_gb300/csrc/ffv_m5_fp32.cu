@@ -1186,14 +1186,20 @@ __device__ __forceinline__ void clamp_zerou_d(const M5Consts &k, double *s, cons
 }
 
 // m5_cell_update of the FP32-flux form: the face fluxes of the partial densities, momentum,
-// energy, volume fractions and internal energies are summed in FP64 (the energy fluxes of
-// opposite faces cancel to ~1e-12 of their size), those of the deformation in FP32; the
-// non-conservative terms (m5_residual.c:175-215) are formed in FP32 from the cell's
-// volume fractions, deformation and material stresses (pressures recovered in FP64) and
-// added to the FP64 residual; the RK stage, positivity, ZEROU and the stage-1 ghost-fluid
-// trigger as in the FP64 form.
+// energy, volume fractions and internal energies are summed exactly, as double-float pairs
+// (the energy fluxes of opposite faces cancel to ~1e-12 of their size: identical fluxes of a
+// quiet region must cancel exactly), those of the deformation in FP32; the
+// non-conservative terms (m5_residual.c:175-215) are formed in FP32 from the cell's volume
+// fractions, deformation and material stresses (pressures recovered in double-float) and
+// added to the pairs.  The residual is then rounded once to FP32 -- an error of 6e-8 of the
+// residual, below the FP32 face fluxes' own rounding of 6e-8 of each flux -- so that the FP64
+// pipe (1/64 of the FP32 rate on GB300) only carries the RK stage: a conversion and one or
+// three fused multiply-adds per variable.  The RK stage, positivity, ZEROU and the stage-1
+// ghost-fluid trigger as in the FP64 form.  RHS receives the entries the ghost-fluid fix
+// reads (partial densities and momentum).
+// three blocks of 128 threads per SM (at most 170 registers)
 template <int N>
-__global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, M5Consts k,
+__global__ void __launch_bounds__(128, 3) m5f_cell_update(ffv_dmesh m, ffv_geom g, M5Consts k,
                                                        const double *__restrict__ S,
                                                        double *__restrict__ SN,
                                                        const float *__restrict__ FF,
@@ -1250,10 +1256,10 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
     avf[i] = a_d.hi;
     eos_stress_f(st_all, avf[i], df_to_float(p), sE, k.mu_f[i], ast[i]);
   }
-  double rhs[NA];
+  df rhs[NA];
   float rhsA[9], nc[N - 1 + N + 9];
 #pragma unroll
-  for (int iv = 0; iv < NA; iv++) rhs[iv] = 0.0;
+  for (int iv = 0; iv < NA; iv++) rhs[iv] = df_make(0.0f);
 #pragma unroll
   for (int q = 0; q < 9; q++) rhsA[q] = 0.0f;
 #pragma unroll
@@ -1273,7 +1279,7 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
       }
     }
 #pragma unroll
-    for (int iv = 0; iv < NA; iv++) rhs[iv] += (double)(sg * FF[((int64_t)ff * C::NEQ + iv) * m.n + fc]);
+    for (int iv = 0; iv < NA; iv++) rhs[iv] = df_add_f(rhs[iv], sg * FF[((int64_t)ff * C::NEQ + iv) * m.n + fc]);
 #pragma unroll
     for (int q = 0; q < 9; q++) rhsA[q] += sg * FF[((int64_t)ff * C::NEQ + C::i5 + q) * m.n + fc];
     const float un = sg * UF[((int64_t)ff * 3 + 0) * m.n + fc];
@@ -1306,26 +1312,29 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
     R5[7] += Af * ((C2 * un * nx + C2 * vn * ny) + A2 * un * nz - B2 * vn * nz);
     R5[8] += Af * ((C3 * un * nx + C3 * vn * ny) + A3 * un * nz - B3 * vn * nz);
   }
-  double r[C::NEQ];
 #pragma unroll
-  for (int iv = 0; iv < NA; iv++) r[iv] = rhs[iv];
+  for (int iv = 0; iv < N - 1; iv++) rhs[C::i3 + iv] = df_add_f(rhs[C::i3 + iv], nc[iv]);
 #pragma unroll
-  for (int iv = 0; iv < N - 1; iv++) r[C::i3 + iv] += (double)nc[iv];
+  for (int iv = 0; iv < N; iv++) rhs[C::i4 + iv] = df_add_f(rhs[C::i4 + iv], nc[N - 1 + iv]);
+  float r[C::NEQ];
 #pragma unroll
-  for (int iv = 0; iv < N; iv++) r[C::i4 + iv] += (double)nc[N - 1 + iv];
+  for (int iv = 0; iv < NA; iv++) r[iv] = df_to_float(rhs[iv]);
 #pragma unroll
-  for (int q = 0; q < 9; q++) r[C::i5 + q] = (double)(rhsA[q] + nc[2 * N - 1 + q]);
+  for (int q = 0; q < 9; q++) r[C::i5 + q] = rhsA[q] + nc[2 * N - 1 + q];
   // a non-positive density in the stage's input is reported (the arithmetic is untouched)
   double rho_in = 0.0;
 #pragma unroll
   for (int v = 0; v < N; ++v) rho_in += s[C::i0 + v];
   unsigned st = rho_in <= 0.0 ? FFV_ST_NEG_DENSITY : 0u;
+  double rd[C::NEQ];
 #pragma unroll
   for (int iv = 0; iv < C::NEQ; iv++) {
     if (isnan(r[iv])) st |= FFV_ST_NAN;
-    RHS[(int64_t)iv * m.n + c] = r[iv];
+    rd[iv] = (double)r[iv];
   }
-  const double dt = *dtp, V = g.vol[l], iV = g.inv_vol[l];
+#pragma unroll
+  for (int iv = 0; iv < C::i2; iv++) RHS[(int64_t)iv * m.n + c] = rd[iv];
+  const double dtiV = *dtp * g.inv_vol[l];
   double sn[C::NEQ];
   if (irk == 1) {
 #pragma unroll
@@ -1343,25 +1352,24 @@ __global__ void __launch_bounds__(128) m5f_cell_update(ffv_dmesh m, ffv_geom g, 
       if (k.mu[v] != 0.0) {
         const int e = C::i3 + v;
         const double phi_old = s[e] - k.avf_lim;
-        const double as_new = sn[e] + dt * (iV * r[e]);
+        const double as_new = fma(dtiV, rd[e], sn[e]);
         if (phi_old * (as_new - k.avf_lim) < 0.0) gfm = true;
       }
     }
 #pragma unroll
     for (int e = 0; e < C::NEQ; e++)
-      if (!gfm || e >= C::i2) s[e] = sn[e] + dt * (iV * r[e]);
+      if (!gfm || e >= C::i2) s[e] = fma(dtiV, rd[e], sn[e]);
   } else {
     const double a = irk == 2 ? 3.0 / 4.0 : (irk == 3 ? 1.0 / 3.0 : 1.0 / 2.0);
     const double b = 1.0 - a;
 #pragma unroll
-    for (int e = 0; e < C::NEQ; e++) s[e] = a * sn[e] + b * s[e] + b * dt * r[e] * iV;
+    for (int e = 0; e < C::NEQ; e++) s[e] = fma(a, sn[e], b * fma(dtiV, rd[e], s[e]));
   }
   if (!gfm) clamp_zerou_d<N>(k, s, sn);
 #pragma unroll
   for (int e = 0; e < C::NEQ; e++) Snew[(int64_t)e * m.n + c] = s[e];
   flag[c] = gfm ? 1 : 0;
   if (st) atomicOr(status, st);
-  (void)V;
 }
 
 template <int N>
