@@ -240,7 +240,9 @@ void ffv_fill_geom(const ffv_mesh *m, ffv_geom *g) {
       g->dcf_f[l][q] = (float)g->dcf[l][q];
       g->idcc_f[l][q] = (float)(1.0 / g->dcc[l][q]);
     }
+    g->area_f[l] = (float)g->area[l];
   }
+  for (int l = 1; l <= FFV_MAX_LEVEL; l++) g->area4_fine_f[l] = (float)(4.0 * g->area[l + 1]);
 }
 
 // a read-only view of a context for the indicator (ffv_mlp.cu)

@@ -34,6 +34,10 @@ struct ffv_geom {
   // FP32 forms for the FP32-flux reconstruction: dcf and 1 / dcc (inf at a boundary)
   float dcf_f[FFV_MAX_LEVEL + 2][4];
   float idcc_f[FFV_MAX_LEVEL + 2][4];
+  // FP32 face areas of the FP32-flux form: a level's own, and 4 x the next finer level's
+  // (the four sub-faces of a face towards finer neighbours)
+  float area_f[FFV_MAX_LEVEL + 2];
+  float area4_fine_f[FFV_MAX_LEVEL + 2];
 };
 
 __device__ __forceinline__ int face_class(uint32_t kind) { return (kind & FFV_FK_BC) ? 3 : (int)kind; }

@@ -11,6 +11,7 @@
 // this way must stay within about 1e-38..3e38 (energies ~1e11, pressures ~1e10, fractions
 // >= 1e-8 here).
 #pragma once
+#include "ffv_cvt.cuh"
 
 struct df {
   float hi, lo;
@@ -18,10 +19,11 @@ struct df {
 
 __device__ __forceinline__ df df_make(float a) { return df{a, 0.0f}; }
 
-// the nearest double-float of an FP64 value (a conversion: FP64 pipe, used once per value)
+// the nearest double-float of an FP64 value (the conversions on the integer pipe,
+// ffv_cvt.cuh)
 __host__ __device__ __forceinline__ df df_from_double(double x) {
-  const float h = (float)x;
-  return df{h, (float)(x - (double)h)};
+  const float h = f32_of_f64(x);
+  return df{h, f32_low_of_f64(x, h)};
 }
 
 __device__ __forceinline__ df fast_two_sum(float a, float b) {  // |a| >= |b|

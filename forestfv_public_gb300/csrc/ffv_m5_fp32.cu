@@ -31,6 +31,7 @@
 // form is measured instead).
 #include <math.h>
 
+#include "ffv_cvt.cuh"
 #include "ffv_device.cuh"
 #include "ffv_m5.cuh"
 #include "ffv_m5_frame.cuh"
@@ -135,7 +136,7 @@ __device__ __forceinline__ void eos_stress_f(float st[3][3], float avf, float pr
 
 // D of an FP64 deformation tensor: A - I formed in FP64, then rounded
 __device__ __forceinline__ float dev_of(const double *A, int q) {
-  return (float)(A[q] - ((q == 0 || q == 4 || q == 8) ? 1.0 : 0.0));
+  return f32_of_f64(A[q] - ((q == 0 || q == 4 || q == 8) ? 1.0 : 0.0));
 }
 
 // A of a deviation, for the advection of A (there relative FP32 precision of A is enough)
@@ -515,7 +516,7 @@ __device__ void write_record(const M5Consts &k, const double *V, const double *p
   }
   at[N - 1] = 1.0 - sum;
 #pragma unroll
-  for (int i = 0; i < C::i5; i++) out[i * stride] = (float)V[i];
+  for (int i = 0; i < C::i5; i++) out[i * stride] = f32_of_f64(V[i]);
 #pragma unroll
   for (int q = 0; q < 9; q++) out[(C::i5 + q) * stride] = dev_of(V + C::i5, q);
 #pragma unroll
@@ -888,7 +889,7 @@ __device__ unsigned relax_cell_df(const M5Consts &k, double *V) {
   // and the critical slots as pairs
   float v[C::NEQ];
 #pragma unroll
-  for (int i = 0; i < C::i5; i++) v[i] = (float)V[i];
+  for (int i = 0; i < C::i5; i++) v[i] = f32_of_f64(V[i]);
 #pragma unroll
   for (int q = 0; q < 9; q++) v[C::i5 + q] = dev_of(V + C::i5, q);
   df cr[2 * N];
@@ -901,11 +902,11 @@ __device__ unsigned relax_cell_df(const M5Consts &k, double *V) {
   df ratio;
   const unsigned st = relax_face_df<N>(k, v, cr, p_eq, &ratio);
 #pragma unroll
-  for (int iv = 0; iv < N - 1; ++iv) V[C::i3 + iv] = (double)cr[iv].hi + (double)cr[iv].lo;
+  for (int iv = 0; iv < N - 1; ++iv) V[C::i3 + iv] = f64_of_f32(cr[iv].hi) + f64_of_f32(cr[iv].lo);
 #pragma unroll
   for (int iv = 0; iv < N; ++iv)
-    V[C::i4 + iv] = (double)cr[N - 1 + iv].hi + (double)cr[N - 1 + iv].lo;
-  const double r = (double)ratio.hi + (double)ratio.lo;
+    V[C::i4 + iv] = f64_of_f32(cr[N - 1 + iv].hi) + f64_of_f32(cr[N - 1 + iv].lo);
+  const double r = f64_of_f32(ratio.hi) + f64_of_f32(ratio.lo);
 #pragma unroll
   for (int q = 0; q < 9; ++q) V[C::i5 + q] = V[C::i5 + q] * r;
   return st;
@@ -925,7 +926,7 @@ __global__ void __launch_bounds__(256) m5f_shadow(int64_t n, const double *__res
     for (int v = 0; v < C::NEQ; v++) {
       const double x = S[(int64_t)v * n + c] -
                        ((v == C::i5 || v == C::i5 + 4 || v == C::i5 + 8) ? 1.0 : 0.0);
-      const float h = (float)x;
+      const float h = (float)x;  // hardware conversions: this kernel is bound by memory
       Sf[(int64_t)v * n + c] = h;
 #pragma unroll
       for (int j = 0; j < 2 * N; j++)
@@ -1090,7 +1091,7 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
   if (kind == (FFV_FK_BC | FFV_BC_SYMMETRY)) {  // the cell's own state (m5_hllc.c:59-63)
     record_of_cell<N>(k, S, m.n, c, U);
     make_sol_f<N>(k, U, 0.0f, L);
-    symmetry_acc_f<F, N>(L, k.flux_form == FFV_FLUX_CONSISTENT, (float)g.area[l], ff, uf);
+    symmetry_acc_f<F, N>(L, k.flux_form == FFV_FLUX_CONSISTENT, g.area_f[l], ff, uf);
     return;
   }
   if (k.order == 2) load_record<N>(SF, m.n, F, c, U);
@@ -1101,11 +1102,11 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
     ghost_f<F, N>(L, bc, R);
     const bool gfm = L.phi0 * R.phi0 < 0.0f;
     if (gfm) gfm_face = 1.0;
-    st |= hllc_acc_f<F, N>(k, L, R, bc, gfm, (float)g.area[l], ff, uf);
+    st |= hllc_acc_f<F, N>(k, L, R, bc, gfm, g.area_f[l], ff, uf);
     return;
   }
   const int nsub = kind == FFV_FK_FINER ? 4 : 1;
-  const float A = (float)(kind == FFV_FK_FINER ? g.area[l + 1] : g.area[l]);
+  const float A = kind == FFV_FK_FINER ? g.area_f[l + 1] : g.area_f[l];
   const int32_t *sg = kind == FFV_FK_FINER ? m.sub + 4 * (int64_t)m.nbr[(int64_t)F * m.n + c] : nullptr;
 #pragma unroll 1
   for (int q = 0; q < nsub; q++) {
@@ -1217,28 +1218,30 @@ __global__ void __launch_bounds__(128, 3) m5f_cell_update(ffv_dmesh m, ffv_geom 
   const int l = ffv_info_level(info);
   double s[C::NEQ];
   load_state<N>(S, m.n, c, s);
-  // the cell's volume fractions (make_sol, cell form) and material stresses
-  const double lo = k.amin / 100.0, hi = 1.0 - (k.amin / 100.0);
-  double at[N], sum = 0.0;
+  // the cell's volume fractions (make_sol, cell form: clamped to [amin/100, 1 - amin/100],
+  // renormalised when their sum exceeds the upper bound) as double-float pairs, and the
+  // material stresses
+  df at[N], asum = df_make(0.0f);
 #pragma unroll
   for (int i = 0; i < N - 1; ++i) {
-    at[i] = s[C::i3 + i];
-    if (at[i] <= lo) at[i] = lo;
-    else if (at[i] >= hi) at[i] = hi;
-    sum += at[i];
+    df a = df_from_double(s[C::i3 + i]);
+    if (df_le(a, k.alo_d)) a = k.alo_d;
+    else if (df_le(k.ahi_d, a)) a = k.ahi_d;
+    at[i] = a;
+    asum = df_add(asum, a);
   }
-  if (sum > hi) {
-    const double dif = sum - hi;
+  if (df_lt(k.ahi_d, asum)) {
+    const df dif = df_sub(asum, k.ahi_d);
 #pragma unroll
-    for (int j = 0; j < N - 1; ++j) at[j] -= (at[j] / sum) * dif;
-    sum = hi;
+    for (int j = 0; j < N - 1; ++j) at[j] = df_sub(at[j], df_mul(df_div(at[j], asum), dif));
+    asum = k.ahi_d;
   }
-  at[N - 1] = 1.0 - sum;
+  at[N - 1] = df_sub(df_make(1.0f), asum);
   float A[9], D[9], avf[N], ast[N][3][3], st_all[3][3];
 #pragma unroll
   for (int q = 0; q < 9; q++) {
     D[q] = dev_of(s + C::i5, q);
-    A[q] = (float)s[C::i5 + q];
+    A[q] = full_of(D, q);
   }
   StrainF sE;
   strain_f(D, sE);
@@ -1250,7 +1253,7 @@ __global__ void __launch_bounds__(128, 3) m5f_cell_update(ffv_dmesh m, ffv_geom 
   for (int i = 0; i < N; ++i) {
     // the material pressure only enters the FP32 stress: recovered in double-float
     const float ael = elastic_energy_f(sE, k.mu_f[i]);
-    const df a_d = df_from_double(at[i]);
+    const df a_d = at[i];
     const df p = df_sub(df_div(df_mul(k.gm1_d[i], df_add_f(df_from_double(s[C::i4 + i]), -ael)), a_d),
                         k.gpi_d[i]);
     avf[i] = a_d.hi;
@@ -1285,7 +1288,7 @@ __global__ void __launch_bounds__(128, 3) m5f_cell_update(ffv_dmesh m, ffv_geom 
     const float un = sg * UF[((int64_t)ff * 3 + 0) * m.n + fc];
     const float vn = sg * UF[((int64_t)ff * 3 + 1) * m.n + fc];
     const float wn = sg * UF[((int64_t)ff * 3 + 2) * m.n + fc];
-    const float Af = (float)(kind == FFV_FK_FINER ? 4.0 * g.area[l + 1] : g.area[l]);
+    const float Af = kind == FFV_FK_FINER ? g.area4_fine_f[l] : g.area_f[l];
     const int ax = fr_n_axis(F);
     const float nn[3] = {ax == 0 ? (float)fr_n_sign(F) : 0.0f, ax == 1 ? (float)fr_n_sign(F) : 0.0f,
                          ax == 2 ? (float)fr_n_sign(F) : 0.0f};
@@ -1330,7 +1333,7 @@ __global__ void __launch_bounds__(128, 3) m5f_cell_update(ffv_dmesh m, ffv_geom 
 #pragma unroll
   for (int iv = 0; iv < C::NEQ; iv++) {
     if (isnan(r[iv])) st |= FFV_ST_NAN;
-    rd[iv] = (double)r[iv];
+    rd[iv] = f64_of_f32(r[iv]);
   }
 #pragma unroll
   for (int iv = 0; iv < C::i2; iv++) RHS[(int64_t)iv * m.n + c] = rd[iv];
@@ -1406,9 +1409,9 @@ __global__ void __launch_bounds__(128) m5f_indicator_fields(int64_t n, M5Consts 
   if (c >= n) return;
   float r = 0.0f;
 #pragma unroll
-  for (int iv = 0; iv < N; ++iv) r += (float)S[(int64_t)(C::i0 + iv) * n + c];
-  const float mx = (float)S[(int64_t)C::i1 * n + c], my = (float)S[(int64_t)(C::i1 + 1) * n + c],
-              mz = (float)S[(int64_t)(C::i1 + 2) * n + c];
+  for (int iv = 0; iv < N; ++iv) r += f32_of_f64(S[(int64_t)(C::i0 + iv) * n + c]);
+  const float mx = f32_of_f64(S[(int64_t)C::i1 * n + c]), my = f32_of_f64(S[(int64_t)(C::i1 + 1) * n + c]),
+              mz = f32_of_f64(S[(int64_t)(C::i1 + 2) * n + c]);
   df at[N];
 #pragma unroll
   for (int i = 0; i < N - 1; ++i) at[i] = df_from_double(S[(int64_t)(C::i3 + i) * n + c]);
@@ -1420,7 +1423,7 @@ __global__ void __launch_bounds__(128) m5f_indicator_fields(int64_t n, M5Consts 
   float D[9];
 #pragma unroll
   for (int q = 0; q < 9; q++)
-    D[q] = (float)(S[(int64_t)(C::i5 + q) * n + c] - ((q == 0 || q == 4 || q == 8) ? 1.0 : 0.0));
+    D[q] = f32_of_f64(S[(int64_t)(C::i5 + q) * n + c] - ((q == 0 || q == 4 || q == 8) ? 1.0 : 0.0));
   StrainF sE;
   strain_f(D, sE);
   float st[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};

@@ -15,6 +15,7 @@
 #pragma once
 #include <math.h>
 
+#include "ffv_cvt.cuh"
 #include "ffv_m5.cuh"
 
 __device__ inline void plastic_jacobi3(const double G[9], double lam[3], double Q[9]) {
@@ -75,7 +76,7 @@ __device__ inline double plastic_vm(double mu, double m, const double d[3], doub
 // of |G| mu, is far below the 1 % margin the caller leaves)
 __device__ inline float plastic_vm_screen(const double *A, float mu) {
   float a[9], G[9];
-  for (int q = 0; q < 9; q++) a[q] = (float)A[q];
+  for (int q = 0; q < 9; q++) a[q] = f32_of_f64(A[q]);
   // a fluid cell carries A = 0 (G = 0, no elastic stress): nothing to screen
   if (a[0] == 0.0f && a[4] == 0.0f && a[8] == 0.0f && a[1] == 0.0f && a[2] == 0.0f &&
       a[3] == 0.0f && a[5] == 0.0f && a[6] == 0.0f && a[7] == 0.0f)
