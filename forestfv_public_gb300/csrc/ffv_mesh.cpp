@@ -175,25 +175,30 @@ static int mesh_build(const ffv_forest_desc *desc, int64_t nleaves, const int32_
 
   const int nthreads = host_threads();
   std::vector<int> tmin(nthreads, FFV_MAX_LEVEL), tmax(nthreads, 1), terr(nthreads, FFV_OK);
+  // per-thread results in locals, stored once (the threads' slots share cache lines)
   parallel_chunks(nleaves, nthreads, [&](int t, int64_t c0, int64_t c1) {
-    for (int64_t i = c0; i < c1 && terr[t] == FFV_OK; i++) {
+    int err = FFV_OK, lo = FFV_MAX_LEVEL, hi = 1;
+    for (int64_t i = c0; i < c1 && err == FFV_OK; i++) {
       int l = level[i];
       if (l < 1 || l > FFV_MAX_LEVEL) {
-        terr[t] = FFV_ERR_TABLE;
+        err = FFV_ERR_TABLE;
         break;
       }
-      tmin[t] = std::min(tmin[t], l);
-      tmax[t] = std::max(tmax[t], l);
+      lo = std::min(lo, l);
+      hi = std::max(hi, l);
       const int32_t ext = 1 << (l - 1);
       for (int a = 0; a < 3; a++)
         if (tree_ijk[3 * i + a] < 0 || tree_ijk[3 * i + a] >= T[a] || cell_ijk[3 * i + a] < 0 ||
             cell_ijk[3 * i + a] >= ext)
-          terr[t] = FFV_ERR_TABLE;
+          err = FFV_ERR_TABLE;
       // global coordinates at the leaf level must fit the 21-bit Morton lanes
-      if (terr[t] == FFV_OK && ((int64_t)T[0] * ext > (1 << 21) || (int64_t)T[1] * ext > (1 << 21) ||
-                                (int64_t)T[2] * ext > (1 << 21)))
-        terr[t] = FFV_ERR_UNSUPPORTED;
+      if (err == FFV_OK && ((int64_t)T[0] * ext > (1 << 21) || (int64_t)T[1] * ext > (1 << 21) ||
+                            (int64_t)T[2] * ext > (1 << 21)))
+        err = FFV_ERR_UNSUPPORTED;
     }
+    terr[t] = err;
+    tmin[t] = lo;
+    tmax[t] = hi;
   });
   int lmin = FFV_MAX_LEVEL, lmax = 1;
   for (int t = 0; t < nthreads; t++) {
@@ -223,18 +228,22 @@ static int mesh_build(const ffv_forest_desc *desc, int64_t nleaves, const int32_
   // leaves given in canonical order (a regrid's output) need no sort
   std::vector<char> unsorted(nthreads, 0), overlap(nthreads, 0);
   parallel_chunks(nleaves > 0 ? nleaves - 1 : 0, nthreads, [&](int t, int64_t a, int64_t b) {
-    for (int64_t i = a; i < b && !unsorted[t]; i++) unsorted[t] = before(i + 1, i);
+    bool u = false;
+    for (int64_t i = a; i < b && !u; i++) u = before(i + 1, i);
+    unsorted[t] = u;
   });
   if (std::any_of(unsorted.begin(), unsorted.end(), [](char x) { return x != 0; }))
     std::sort(perm.begin(), perm.end(), before);
   // overlap check: a leaf's key range must end before the next leaf of the same tree starts
   parallel_chunks(nleaves > 0 ? nleaves - 1 : 0, nthreads, [&](int t, int64_t c0, int64_t c1) {
-    for (int64_t k = c0; k < c1 && !overlap[t]; k++) {
+    bool ov = false;
+    for (int64_t k = c0; k < c1 && !ov; k++) {
       int64_t a = perm[k], b = perm[k + 1];
       if (tkey[a] != tkey[b]) continue;
       uint64_t span = 1ULL << (3 * (D - (level[a] - 1)));
-      if (lkey[a] + span > lkey[b]) overlap[t] = 1;
+      if (lkey[a] + span > lkey[b]) ov = true;
     }
+    overlap[t] = ov;
   });
   if (std::any_of(overlap.begin(), overlap.end(), [](char x) { return x != 0; }))
     return FFV_ERR_TABLE;

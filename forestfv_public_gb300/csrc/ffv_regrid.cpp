@@ -221,12 +221,15 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
   std::vector<std::vector<int32_t>> csub(nth);
   std::vector<int> crc(nth, FFV_OK);
   std::vector<int> tmin(nth, FFV_MAX_LEVEL + 1), tmax(nth, 0);
+  // per-thread results are kept in locals and stored once: the threads' slots share cache
+  // lines, and writing them per leaf made every store a coherence miss
   parallel_chunks(nn, nth, [&](int t, int64_t a, int64_t b) {
     std::vector<int32_t> &sub = csub[t];
-    for (int64_t j = a; j < b && crc[t] == FFV_OK; j++) {
+    int lmin = FFV_MAX_LEVEL + 1, lmax = 0, err = FFV_OK;
+    for (int64_t j = a; j < b && err == FFV_OK; j++) {
       const int l = L.lev[j];
-      tmin[t] = std::min(tmin[t], l);
-      tmax[t] = std::max(tmax[t], l);
+      lmin = std::min(lmin, l);
+      lmax = std::max(lmax, l);
       const int64_t s = L.src[j];
       if (s >= 0 && copyable(s)) {  // the old rows, renumbered
         const uint32_t info = m->info[s];
@@ -273,22 +276,22 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
             // the region is refined (its first corner may lie deeper on the far side); the
             // four finer neighbours: subface k touches node ffv_face_nodes[f][k] of this face
             int32_t ids[4];
-            for (int k = 0; k < 4 && crc[t] == FFV_OK; k++) {
+            for (int k = 0; k < 4 && err == FFV_OK; k++) {
               const int q = ffv_face_nodes[f][k];
               const int cb[3] = {ffv_corner_x(q), ffv_corner_y(q), ffv_corner_z(q)};
               int64_t fg[3];
               for (int d = 0; d < 3; d++)
                 fg[d] = 2 * g[d] + (d == ax ? (fr.side_dir > 0 ? 0 : 1) : cb[d]);
               const int64_t h2 = find(point_key(l + 1, fg));
-              if (h2 < 0 || L.lev[h2] != l + 1) crc[t] = FFV_ERR_BALANCE;
+              if (h2 < 0 || L.lev[h2] != l + 1) err = FFV_ERR_BALANCE;
               ids[k] = (int32_t)h2;
             }
-            if (crc[t] != FFV_OK) break;
+            if (err != FFV_OK) break;
             kind = FFV_FK_FINER;
             slot = (int32_t)(sub.size() / 4);
             sub.insert(sub.end(), ids, ids + 4);
           } else {
-            crc[t] = FFV_ERR_BALANCE;
+            err = FFV_ERR_BALANCE;
             break;
           }
         }
@@ -297,6 +300,9 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
       }
       nm->info[j] = info;
     }
+    crc[t] = err;
+    tmin[t] = lmin;
+    tmax[t] = lmax;
   });
   rc = FFV_OK;
   for (int t = 0; t < nth && rc == FFV_OK; t++) rc = crc[t];

@@ -255,17 +255,20 @@ extern "C" int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_
   const int nth = host_threads();
   std::vector<int64_t> ns(nth, 0), nm(nth, 0);
   parallel_chunks(m->n, nth, [&](int t, int64_t a, int64_t b) {
+    int64_t s_ = 0, m_ = 0;  // counted in locals: the threads' slots share cache lines
     for (int64_t c = a; c < b; c++) {
       const int32_t l = (int32_t)ffv_info_level(m->info[c]);
-      if (split[c] > l) ns[t]++;
+      if (split[c] > l) s_++;
       // a group merges only if its first leaf (like all eight) wants a coarser level: the
       // group is looked up only then
       if (l > 1 && split[c] < l && ffv_sibling_group(m, c) == c) {
         bool all = true;
         for (int q = 0; q < 8 && all; q++) all = split[c + q] < l;
-        nm[t] += all ? 1 : 0;
+        m_ += all ? 1 : 0;
       }
     }
+    ns[t] = s_;
+    nm[t] = m_;
   });
   *nsplit = 0;
   *nmerge = 0;
