@@ -2,10 +2,12 @@
 stepped `steps` times with one form of the flux, so that an ncu capture can skip the
 launches of the early steps and measure a launch of the developed flow.
 
-  python -m forestfv_public_gb300.profile_case [steps] [reference|consistent]
+  python -m forestfv_public_gb300.profile_case [steps] [reference|consistent] [infer]
 
 Each time step launches the FP32-flux stage kernels twice (RK2); launch k of a kernel belongs
-to step k // 2."""
+to step k // 2.  With `infer`, the learned indicator (random weights, normalised on the
+state) then marks the developed state three times: fields + the fused tcgen05 inference,
+launches 0-2 of mlp_infer_tc."""
 from __future__ import annotations
 
 import os
@@ -30,6 +32,19 @@ def main() -> None:
     s.step(dt, steps)
     print(f"{mesh.n} cells, {steps} steps of the FP32-flux form ({form} flux) in "
           f"{time.perf_counter() - t0:.3f} s")
+    if len(sys.argv) > 3 and sys.argv[3] == "infer":
+        import numpy as np
+        import torch
+        from .indicator import Indicator
+        ind = Indicator(seed=3)
+        F = ind.fields(s).cpu().numpy().astype(np.float64)
+        ind.set_norm(F.mean(axis=1), F.std(axis=1) + 1e-3)
+        marks = torch.zeros(mesh.n, dtype=torch.uint8, device=f"cuda:{s.device}")
+        for _ in range(3):
+            ind.mark(s, 0.5, marks, True)
+        s.sync()
+        print(f"{int(marks.sum())} cells marked")
+        ind.close()
     s.close()
 
 
