@@ -380,6 +380,8 @@ int ffv_create(ffv_ctx **out, const ffv_params *p, int device) {
     }
     k.alo_f = (float)(p->amin / 100.0);
     k.ahi_f = (float)(1.0 - (p->amin / 100.0));
+    k.avf_lim_f = (float)k.avf_lim;
+    k.phi_pair = (k.nsolids == 2 && k.mu[0] != 0.0) ? 1 : 0;
     k.alo_d = df_from_double(p->amin / 100.0);
     k.ahi_d = df_from_double(1.0 - (p->amin / 100.0));
     k.a2lo_d = df_from_double(1.0 - (2.0 * (p->amin / 100.0)));

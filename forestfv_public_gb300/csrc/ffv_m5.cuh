@@ -24,6 +24,10 @@ struct M5Consts {
   float pinf_f[FFV_MAX_MATERIALS], igam_f[FFV_MAX_MATERIALS], mu_f[FFV_MAX_MATERIALS],
       gamma_f[FFV_MAX_MATERIALS], plo_f[FFV_MAX_MATERIALS], preset_f[FFV_MAX_MATERIALS];
   float alo_f, ahi_f;
+  // AVF_LIM in FP32, and whether phi0 takes the larger of two solid fractions (two solids,
+  // the first one elastic): the FP32-flux form's phi0 needs no FP64 instruction
+  float avf_lim_f;
+  int phi_pair;
   // (a - j) / (j + 1), j = 1..6, a = -1 / gamma: the FP32 Newton iteration's binomial series
   float bin_f[FFV_MAX_MATERIALS][6];
   // double-float pairs for the FP32-flux form's pressure recovery: gamma - 1, gamma p_inf,

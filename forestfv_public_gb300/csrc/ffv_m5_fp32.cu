@@ -56,10 +56,12 @@ struct RecL {
 // tr((G - |G|^(1/3) I)^2) = tr((E - g I)^2) and the stress deviator
 // G^2 - tr(G^2)/3 I - |G|^(1/3) (G - tr G/3 I) = (1 - g) dev E + dev(E^2), g = |G|^(1/3) - 1.
 struct StrainF {
-  float E[6];  // G - I (symmetric): E00, E11, E22, E01, E02, E12
-  float g;     // |G|^(1/3) - 1
-  float g16;   // |G|^(1/6)
-  bool solid;  // |G| != 0 (a fluid cell carries A = 0: no elastic stress)
+  float E[6];    // G - I (symmetric): E00, E11, E22, E01, E02, E12
+  float g;       // |G|^(1/3) - 1
+  float ig16;    // |G|^(-1/6)
+  float tr2;     // tr((E - g I)^2)
+  float dev[6];  // (1 - g) dev E + dev(E^2), by stress_deviator_f
+  bool solid;    // |G| != 0 (a fluid cell carries A = 0: no elastic stress)
 };
 
 // slot of E_ij in StrainF::E
@@ -67,6 +69,8 @@ __host__ __device__ constexpr int esym(int i, int j) {
   return i == j ? i : (i + j == 1 ? 3 : (i + j == 2 ? 4 : 5));
 }
 
+// E, |G|^(1/3) - 1, |G|^(-1/6) and tr((E - g I)^2) of a deviation D: the material-independent
+// parts of every material's elastic energy (the materials differ by their shear modulus only)
 __device__ __forceinline__ void strain_f(const float D[9], StrainF &s) {
 #pragma unroll
   for (int i = 0; i < 3; i++)
@@ -80,47 +84,53 @@ __device__ __forceinline__ void strain_f(const float D[9], StrainF &s) {
                    e02 * (e01 * e12 - e11 * e02);
   const float x = (e00 + e11 + e22) + m2 + dE;  // |G| - 1
   s.solid = (1.0f + x) != 0.0f;
+  float g16;
   if (fabsf(x) <= 0.03125f) {
     // (1 + x)^(1/3) - 1 by its binomial series to x^5 (coefficients 1/3, -1/9, 5/81,
     // -10/243, 22/729); the first omitted term is below 2e-9 of the sum for |x| <= 1/32
     s.g = x * (1.0f / 3.0f + x * (-1.0f / 9.0f + x * (5.0f / 81.0f + x * (-10.0f / 243.0f + x * (22.0f / 729.0f)))));
-    s.g16 = sqrtf(1.0f + s.g);
+    g16 = sqrtf(1.0f + s.g);
   } else {
     const float g13 = cbrtf(fabsf(1.0f + x));
     s.g = g13 - 1.0f;
-    s.g16 = sqrtf(g13);
+    g16 = sqrtf(g13);
   }
+  s.ig16 = 1.0f / g16;
+  const float d0 = e00 - s.g, d1 = e11 - s.g, d2 = e22 - s.g;
+  s.tr2 = d0 * d0 + d1 * d1 + d2 * d2 + 2.0f * (e01 * e01 + e02 * e02 + e12 * e12);
+}
+
+// the stress deviator's material-independent factor (1 - g) dev E + dev(E^2) into s.dev
+__device__ __forceinline__ void stress_deviator_f(StrainF &s) {
+  const float *E = s.E;
+  float E2[6];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = i; j < 3; j++)
+      E2[esym(i, j)] = E[esym(i, 0)] * E[esym(0, j)] + E[esym(i, 1)] * E[esym(1, j)] +
+                       E[esym(i, 2)] * E[esym(2, j)];
+  const float J1 = (E[0] + E[1] + E[2]) * (1.0f / 3.0f), J2 = (E2[0] + E2[1] + E2[2]) * (1.0f / 3.0f);
+  const float a = 1.0f - s.g;
+#pragma unroll
+  for (int q = 0; q < 6; q++) s.dev[q] = q < 3 ? a * (E[q] - J1) + (E2[q] - J2) : a * E[q] + E2[q];
 }
 
 // e_el = mu / (4 |G|^(1/6)) tr((G - |G|^(1/3) I)^2)   (state_equation.c:269-317)
 __device__ __forceinline__ float elastic_energy_f(const StrainF &s, float mu) {
   if (!s.solid || !(mu != 0.0f)) return 0.0f;
-  const float *E = s.E;
-  const float d0 = E[0] - s.g, d1 = E[1] - s.g, d2 = E[2] - s.g;
-  const float tr = d0 * d0 + d1 * d1 + d2 * d2 + 2.0f * (E[3] * E[3] + E[4] * E[4] + E[5] * E[5]);
-  return mu / (4.0f * s.g16) * tr;
+  return (0.25f * mu) * s.ig16 * s.tr2;
 }
 
 // material stress -alpha p I - mu/|G|^(1/6) ((1 - g) dev E + dev(E^2)), accumulated into st
-// (state_equation.c:143-204 in the E form)
+// (state_equation.c:143-204 in the E form; s.dev from stress_deviator_f)
 __device__ __forceinline__ void eos_stress_f(float st[3][3], float avf, float pr, const StrainF &e,
                                              float mu, float (*ast)[3]) {
   float s[6];
   if (e.solid && (mu != 0.0f)) {
-    const float *E = e.E;
-    float E2[6];
+    const float f = mu * e.ig16;
 #pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = i; j < 3; j++)
-        E2[esym(i, j)] = E[esym(i, 0)] * E[esym(0, j)] + E[esym(i, 1)] * E[esym(1, j)] +
-                         E[esym(i, 2)] * E[esym(2, j)];
-    const float J1 = (E[0] + E[1] + E[2]) * (1.0f / 3.0f), J2 = (E2[0] + E2[1] + E2[2]) * (1.0f / 3.0f);
-    const float a = 1.0f - e.g;
-    const float f = mu / e.g16;
-#pragma unroll
-    for (int q = 0; q < 6; q++)
-      s[q] = q < 3 ? -avf * pr - f * (a * (E[q] - J1) + (E2[q] - J2)) : -f * (a * E[q] + E2[q]);
+    for (int q = 0; q < 6; q++) s[q] = q < 3 ? -avf * pr - f * e.dev[q] : -f * e.dev[q];
   } else {
 #pragma unroll
     for (int q = 0; q < 6; q++) s[q] = q < 3 ? -avf * pr : 0.0f;
@@ -183,6 +193,7 @@ __device__ void make_sol_f(const M5Consts &k, const float *U, float phi0, SolF<N
   for (int q = 0; q < 9; q++) s.D[q] = U[C::i5 + q];
   StrainF sE;
   strain_f(s.D, sE);
+  stress_deviator_f(sE);
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -231,8 +242,8 @@ __device__ __forceinline__ float cell_phi0_f(const M5Consts &k, const float *__r
     else if (a <= k.alo_f) a = k.alo_f;
     ac[i] = a;
   }
-  const float lim = (float)k.avf_lim;
-  if (N > 2 && k.nsolids == 2 && k.mu[0] != 0.0)
+  const float lim = k.avf_lim_f;
+  if (N > 2 && k.phi_pair)
     return ((ac[0] > ac[N > 2 ? 1 : 0]) ? ac[0] : ac[N > 2 ? 1 : 0]) - lim;
   return ac[0] - lim;
 }
@@ -261,8 +272,8 @@ struct NCf {
 // never as U*_K minus U_K: the solid's total energy is ~5e10 J/m^3 (p_inf 3.2e10), whose FP32
 // ulp (4096) would otherwise enter every face's energy flux as noise even at rest.
 template <int F, int N>
-__device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const SolF<N> &L,
-                                  const SolF<N> &R, bool leftside, float u_S, float SL, float SR,
+__device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, float rL, float rR,
+                                  bool both_solid, bool leftside, float u_S, float SL, float SR,
                                   float uL, float vL, float wL, float uR, float vR, float wR,
                                   const float sL[3], const float sR[3], float *dU, NCf<N> &nc) {
   using C = K5<N>;
@@ -279,11 +290,11 @@ __device__ unsigned star_region_f(const M5Consts &k, const SolF<N> &s, const Sol
     ar_S[v] = s.ra[v] * q;
     r_S += ar_S[v];
   }
-  const float mR = (uR - SR) * R.r, mL = (uL - SL) * L.r;
+  const float mR = (uR - SR) * rR, mL = (uL - SL) * rL;
   const float iden = 1.0f / (mR - mL);
   const float s11_S = (mR * sL[0] - mL * sR[0] + mL * mR * (uR - uL)) * iden;
   float s12_S = 0.0f, s13_S = 0.0f;
-  if ((L.phi0 > 0.0f) && (R.phi0 > 0.0f)) {
+  if (both_solid) {
     s12_S = (mR * sL[1] - mL * sR[1] + mL * mR * (vR - vL)) * iden;
     s13_S = (mR * sL[2] - mL * sR[2] + mL * mR * (wR - wL)) * iden;
   }
@@ -403,7 +414,40 @@ __device__ void flux_n_f(const SolF<N> &s, int flag, bool gfm, bool cons, NCf<N>
   for (int q = 0; q < 9; q++) Fn[C::i5 + q] = sgn<sg>(ua * nc.A[q]);
 }
 
-// m5_hllc.c:3-95 / m5_hllc_gfm.c:3-100 in FP32: ff += A (F.n + corr)
+// K = a ? A : B, field by field (selects: the states stay in registers)
+template <int N>
+__device__ __forceinline__ void select_sol(bool a, const SolF<N> &A, const SolF<N> &B, SolF<N> &K) {
+  K.r = a ? A.r : B.r;
+  K.u = a ? A.u : B.u;
+  K.v = a ? A.v : B.v;
+  K.w = a ? A.w : B.w;
+  K.e = a ? A.e : B.e;
+  K.ut = a ? A.ut : B.ut;
+  K.vt = a ? A.vt : B.vt;
+  K.wt = a ? A.wt : B.wt;
+  K.c2 = a ? A.c2 : B.c2;
+  K.phi0 = a ? A.phi0 : B.phi0;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    K.ra[i] = a ? A.ra[i] : B.ra[i];
+    K.avf[i] = a ? A.avf[i] : B.avf[i];
+    K.are[i] = a ? A.are[i] : B.are[i];
+    K.p[i] = a ? A.p[i] : B.p[i];
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) K.D[q] = a ? A.D[q] : B.D[q];
+#pragma unroll
+  for (int i = 0; i < 3; i++)
+#pragma unroll
+    for (int j = 0; j < 3; j++) K.st[i][j] = a ? A.st[i][j] : B.st[i][j];
+#pragma unroll
+  for (int q = 0; q < K5<N>::NC; q++) K.vec[q] = a ? A.vec[q] : B.vec[q];
+}
+
+// m5_hllc.c:3-95 / m5_hllc_gfm.c:3-100 in FP32: ff += A (F.n + corr).  The solver's four
+// branches share one star-region and one physical-flux evaluation on the state of the
+// contact's upwind side (one inlined copy of each: the kernel is large enough for the
+// instruction cache to matter)
 template <int F, int N>
 __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, bool gfm,
                                float Area, float *ff, float unc[3]) {
@@ -443,26 +487,27 @@ __device__ unsigned hllc_acc_f(const M5Consts &k, SolF<N> L, SolF<N> R, int bc, 
   for (int iv = 0; iv < C::NC; ++iv) corr[iv] = 0.0f;
   const bool left_star = gfm ? (SL < 0.0f && 0.0f <= u_S) : (SL <= 0.0f && 0.0f <= u_S);
   const bool right_star = gfm ? (u_S < 0.0f && 0.0f < SR) : (u_S <= 0.0f && 0.0f <= SR);
-  if (0.0f <= SL) {
-    flux_n_f<F>(L, 0, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
-  } else if (left_star) {
-    st |= star_region_f<F>(k, L, L, R, true, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, dU, nc);
-    flux_n_f<F>(L, 1, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
-#pragma unroll
-    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SL * dU[iv];
-  } else if (right_star) {
-    st |= star_region_f<F>(k, R, L, R, false, u_S, SL, SR, uL, vL, wL, uR, vR, wR, sL, sR, dU, nc);
-    flux_n_f<F>(R, 2, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
-#pragma unroll
-    for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SR * dU[iv];
-  } else if (SR <= 0.0f) {
-    flux_n_f<F>(R, 3, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
-  } else {
+  // 0: supersonic from the left, 1: left star state, 2: right star state, 3: supersonic
+  // from the right
+  const int branch = (0.0f <= SL) ? 0 : left_star ? 1 : right_star ? 2 : (SR <= 0.0f) ? 3 : -1;
+  if (branch < 0) {
     st |= FFV_ST_NO_BRANCH;
 #pragma unroll
     for (int iv = 0; iv < C::NEQ; ++iv) Fn[iv] = 0.0f;
 #pragma unroll
     for (int d = 0; d < 3; d++) nc.unc[d] = 0.0f;
+  } else {
+    const bool left = branch <= 1;
+    SolF<N> K;
+    select_sol<N>(left, L, R, K);
+    if (branch == 1 || branch == 2) {
+      st |= star_region_f<F>(k, K, L.r, R.r, (L.phi0 > 0.0f) && (R.phi0 > 0.0f), left, u_S, SL,
+                             SR, uL, vL, wL, uR, vR, wR, sL, sR, dU, nc);
+      const float SK = left ? SL : SR;
+#pragma unroll
+      for (int iv = 0; iv < C::NC; ++iv) corr[iv] = SK * dU[iv];
+    }
+    flux_n_f<F>(K, branch, gfm, k.flux_form == FFV_FLUX_CONSISTENT, nc, Fn);
   }
 #pragma unroll
   for (int iv = 0; iv < C::NEQ; ++iv) ff[iv] += Area * (Fn[iv] + (iv < C::NC ? corr[iv] : 0.0f));
@@ -1097,28 +1142,29 @@ __device__ void face_flux_f(const ffv_dmesh &m, const ffv_geom &g, const M5Const
   if (k.order == 2) load_record<N>(SF, m.n, F, c, U);
   else record_of_cell<N>(k, S, m.n, c, U);
   make_sol_f<N>(k, U, Sf ? cell_phi0_f<N>(k, Sf, m.n, c) : (float)cell_phi0<N>(k, S, m.n, c), L);
-  if (kind & FFV_FK_BC) {
-    const int bc = (int)(kind & 7u);
-    ghost_f<F, N>(L, bc, R);
-    const bool gfm = L.phi0 * R.phi0 < 0.0f;
-    if (gfm) gfm_face = 1.0;
-    st |= hllc_acc_f<F, N>(k, L, R, bc, gfm, g.area_f[l], ff, uf);
-    return;
-  }
+  // one solver call site for the boundary (the ghost state) and the interior faces (the
+  // neighbour's record, or each of four finer neighbours' in turn; the face velocity is the
+  // last subface's divided by four, m5_residual.c:163-165)
+  const bool bnd = (kind & FFV_FK_BC) != 0;
+  const int bc = bnd ? (int)(kind & 7u) : 0;
   const int nsub = kind == FFV_FK_FINER ? 4 : 1;
   const float A = kind == FFV_FK_FINER ? g.area_f[l + 1] : g.area_f[l];
   const int32_t *sg = kind == FFV_FK_FINER ? m.sub + 4 * (int64_t)m.nbr[(int64_t)F * m.n + c] : nullptr;
+  const float inv = 1.0f / (float)nsub;
 #pragma unroll 1
   for (int q = 0; q < nsub; q++) {
-    const int64_t o = sg ? sg[q] : m.nbr[(int64_t)F * m.n + c];
-    if (k.order == 2) load_record<N>(SF, m.n, FO, o, U);
-    else record_of_cell<N>(k, S, m.n, o, U);
-    make_sol_f<N>(k, U, Sf ? cell_phi0_f<N>(k, Sf, m.n, o) : (float)cell_phi0<N>(k, S, m.n, o), R);
+    if (bnd) {
+      ghost_f<F, N>(L, bc, R);
+    } else {
+      const int64_t o = sg ? sg[q] : m.nbr[(int64_t)F * m.n + c];
+      if (k.order == 2) load_record<N>(SF, m.n, FO, o, U);
+      else record_of_cell<N>(k, S, m.n, o, U);
+      make_sol_f<N>(k, U, Sf ? cell_phi0_f<N>(k, Sf, m.n, o) : (float)cell_phi0<N>(k, S, m.n, o), R);
+    }
     const bool gfm = L.phi0 * R.phi0 < 0.0f;
     if (gfm) gfm_face = 1.0;
     float un[3];
-    st |= hllc_acc_f<F, N>(k, L, R, 0, gfm, A, ff, un);
-    const float inv = 1.0f / (float)nsub;
+    st |= hllc_acc_f<F, N>(k, L, R, bc, gfm, A, ff, un);
     uf[0] = un[0] * inv;
     uf[1] = un[1] * inv;
     uf[2] = un[2] * inv;
@@ -1245,6 +1291,7 @@ __global__ void __launch_bounds__(128, 3) m5f_cell_update(ffv_dmesh m, ffv_geom 
   }
   StrainF sE;
   strain_f(D, sE);
+  stress_deviator_f(sE);
 #pragma unroll
   for (int i = 0; i < 3; i++)
 #pragma unroll
@@ -1426,6 +1473,7 @@ __global__ void __launch_bounds__(128) m5f_indicator_fields(int64_t n, M5Consts 
     D[q] = f32_of_f64(S[(int64_t)(C::i5 + q) * n + c] - ((q == 0 || q == 4 || q == 8) ? 1.0 : 0.0));
   StrainF sE;
   strain_f(D, sE);
+  stress_deviator_f(sE);
   float st[3][3] = {{0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}, {0.0f, 0.0f, 0.0f}};
   df p = df_make(0.0f);
 #pragma unroll
