@@ -53,6 +53,7 @@ extern "C" int ffv_adapt_changes(const ffv_mesh *m, const int32_t *split, int64_
                                  int64_t *nmerge);
 extern "C" void ffv_mesh_free(ffv_mesh *m);
 int ffv_ctx_mark_state(ffv_ctx *ctx);
+int ffv_ctx_scratch(ffv_ctx *c, double **d_SN, double **d_SF, int64_t *cap, int64_t *cap_nsub);
 
 extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *split,
                              ffv_mesh **out, int64_t *src) {
@@ -81,12 +82,24 @@ extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *spl
   rc = ffv_mesh_adapt(m, split, &nm, cmap);
   if (rc != FFV_OK) return rc;
   const int64_t n_new = nm->n;
-  // carry the state over on the device, then swap the tables
+  // carry the state over on the device, then swap the tables.  When the new mesh fits the
+  // context's buffers (ffv_set_mesh then keeps them), the new state is assembled in the RK
+  // copy and the map in the face-state buffer, both idle between steps: the regrid allocates
+  // nothing on the device.  Otherwise ffv_set_mesh reallocates every buffer, and the remap
+  // uses buffers of its own.
   cudaError_t e = cudaSetDevice(device);
-  int64_t *d_map = nullptr;
-  double *d_T = nullptr;
-  if (e == cudaSuccess) e = cudaMalloc(&d_map, sizeof(int64_t) * n_new);
-  if (e == cudaSuccess) e = cudaMalloc(&d_T, sizeof(double) * neq * n_new);
+  double *d_SN = nullptr, *d_SF = nullptr;
+  int64_t cap = 0, cap_nsub = 0;
+  rc = ffv_ctx_scratch(ctx, &d_SN, &d_SF, &cap, &cap_nsub);
+  if (rc != FFV_OK) {
+    ffv_mesh_free(nm);
+    return rc;
+  }
+  const bool fits = n_new <= cap && (nm->nsub > 0 ? nm->nsub : 1) <= cap_nsub;
+  int64_t *d_map = fits ? reinterpret_cast<int64_t *>(d_SF) : nullptr;
+  double *d_T = fits ? d_SN : nullptr;
+  if (!fits && e == cudaSuccess) e = cudaMalloc(&d_map, sizeof(int64_t) * n_new);
+  if (!fits && e == cudaSuccess) e = cudaMalloc(&d_T, sizeof(double) * neq * n_new);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_map, cmap, sizeof(int64_t) * n_new, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
@@ -112,8 +125,10 @@ extern "C" int ffv_adapt_map(ffv_ctx *ctx, const ffv_mesh *m, const int32_t *spl
       if (e != cudaSuccess) rc = FFV_ERR_CUDA;
     }
   }
-  cudaFree(d_map);
-  cudaFree(d_T);
+  if (!fits) {
+    cudaFree(d_map);
+    cudaFree(d_T);
+  }
   if (rc != FFV_OK) {
     ffv_mesh_free(nm);
     return rc;

@@ -261,6 +261,18 @@ int ffv_ctx_view(ffv_ctx *c, int *device, cudaStream_t *st, ffv_dmesh *dm, const
   return FFV_OK;
 }
 
+// the context's RK copy [neq][cap] and face-state buffer [6 neq][cap] (both idle between
+// steps) and the capacity the mesh buffers are allocated for, for a regrid's state remap
+// (ffv_adapt.cu)
+int ffv_ctx_scratch(ffv_ctx *c, double **d_SN, double **d_SF, int64_t *cap, int64_t *cap_nsub) {
+  if (!c || !c->have_mesh) return FFV_ERR_STATE;
+  *d_SN = c->d_SN;
+  *d_SF = c->d_SF;
+  *cap = c->cap;
+  *cap_nsub = c->cap_nsub;
+  return FFV_OK;
+}
+
 // the context's state for ffv_adapt (ffv_adapt.cu)
 int ffv_ctx_adapt_view(ffv_ctx *c, int *device, cudaStream_t *st, int64_t *n, int *neq,
                        double **d_S, int *model, const M5Consts **k) {
