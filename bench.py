@@ -621,12 +621,16 @@ def gate_medium(kw: dict, dev, counts=(20, 100)) -> dict:
             "pass": all(g["pass"] for g in out)}
 
 
+TRAIN_LMAX, TRAIN_RUNS, TRAIN_WINDOWS = 9, 3, 2  # ~9.5 M cells per snapshot: ~57 M pairs
+
+
 def train_wall_indicator(kw: dict, dev, amr_cfg: dict, seed: int = 20261203):
-    """The indicator of the wall configuration, trained on the GPU on seeded runs of its
-    medium size (levels 4-7) with standoffs U(1.0, 2.5) and bubble radii U(0.05, 0.15):
-    snapshots of (features, "the criterion asks for a finer level within `horizon`
-    steps"), a criterion-driven regrid between snapshots, then AdamW (lr 1e-3, batch
-    8192).  Returns the indicator and a summary."""
+    """The indicator of the wall configuration, trained on the GPU on seeded runs of the
+    configuration's physics on levels 4-9 with standoffs U(1.0, 2.5) and bubble radii
+    U(0.05, 0.15): snapshots of (features, "the criterion asks for a finer level within
+    `horizon` steps") -- TRAIN_RUNS runs of TRAIN_WINDOWS snapshots, about the ~50 M pairs
+    the learned-indicator configuration names -- a criterion-driven regrid between
+    snapshots, then AdamW (lr 1e-3, batch 8192).  Returns the indicator and a summary."""
     import torch
 
     from forestfv_public_gb300 import Solver
@@ -636,24 +640,24 @@ def train_wall_indicator(kw: dict, dev, amr_cfg: dict, seed: int = 20261203):
     t0 = time.perf_counter()
     rng = np.random.default_rng(seed)
     ind = Indicator(device=dev.index, seed=seed)
-    tags7 = wall_tags(7)
-    dt7 = WALL_CFL * (0.5 / (1 << 6)) / C_SOLID
+    tags_t = wall_tags(TRAIN_LMAX)
+    dt_t = WALL_CFL * (0.5 / (1 << (TRAIN_LMAX - 1))) / C_SOLID
     Xs, ys, runs = [], [], 0
-    for k in range(3):
+    for k in range(TRAIN_RUNS):
         standoff, radius = rng.uniform(1.0, 2.5), rng.uniform(0.05, 0.15)
-        mesh, S0, _ = W.bubble_wall_config3(lmax=7, band_cells=4.0, radius=radius,
+        mesh, S0, _ = W.bubble_wall_config3(lmax=TRAIN_LMAX, band_cells=4.0, radius=radius,
                                             standoff=standoff)
         s = Solver(device=dev.index, precision=1, **kw)
         s.set_mesh(mesh)
         s.upload_state(S0)
-        amr = AdaptiveRun(s, tags7)
+        amr = AdaptiveRun(s, tags_t)
         amr.meshadaptation()
         if k == 0:
             mean, std = field_norm([ind.fields(s).cpu().numpy()])
             ind.set_norm(mean, np.maximum(std, np.array([0.05, 0.05, 0.01, 0.01, 1.0],
                                                          np.float32)))
-        for _ in range(3):
-            X, y = collect_window(s, ind, tags7, dt7, amr_cfg["horizon"])
+        for _ in range(TRAIN_WINDOWS):
+            X, y = collect_window(s, ind, tags_t, dt_t, amr_cfg["horizon"])
             Xs.append(X)
             ys.append(y)
             amr.meshadaptation()

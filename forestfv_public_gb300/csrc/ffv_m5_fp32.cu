@@ -843,32 +843,16 @@ __device__ unsigned relax_face_df(const M5Consts &k, float *v, df *cr, float &p_
       // bounds the loop.  Near equilibrium (|x| <= 1/32, most faces away from shocks and
       // interfaces) e_k is the binomial series of (1 + x)^a - 1, a = -1/gamma, to x^7 in
       // Horner form: its first omitted term is below 1e-9 of e_k for gamma >= 1.
-      //
-      // F is convex and decreasing in p, so a Newton step from above the root can overshoot
-      // below every material's pressure floor.  The reference then restarts at the floor
-      // (~1 Pa for a gas) and climbs back by a factor of about 1 + gamma per step -- 19 to 25
-      // iterations for a few percent of the faces next to a gas, and a warp waits for its
-      // slowest face.  Here an overshoot from above the floors moves 1/16 of the way to them
-      // instead: the iterate stays above the floors, reaches the root's side from the left in
-      // a few steps (from the left Newton converges monotonically) and ends on the same root.
       const float F0 = df_to_float(sum0);
-      float pfloor = plo[0];
-#pragma unroll
-      for (int iv = 1; iv < N; ++iv) pfloor = fmaxf(pfloor, plo[iv]);
       float pf = p0, F = 0.0f, dF = 1.0f, prev1 = NAN, prev2 = NAN;
 #pragma unroll 1
       for (int iter = 0; iter < 64; iter++) {
         const float step = F / dF;
         if (iter > 0 && !(fabsf(step) > 1.0e-7f * fabsf(pf))) break;
-        const float pn = pf - step;
-        if (pn < pfloor && pf > pfloor && iter > 0) {
-          pf = pfloor + (pf - pfloor) * 0.0625f;
-        } else {
-          pf = pn;
+        pf = pf - step;
 #pragma unroll
-          for (int iv = 0; iv < N; ++iv)
-            if (pf < plo[iv]) pf = preset[iv];
-        }
+        for (int iv = 0; iv < N; ++iv)
+          if (pf < plo[iv]) pf = preset[iv];
         if (pf == prev1 || pf == prev2) break;
         F = F0;
         dF = 0.0f;

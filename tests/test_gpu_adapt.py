@@ -77,3 +77,28 @@ def test_adapt_model0_copy_and_mean(built_lib):
             i += 1
     assert np.array_equal(Sn, np.array(exp).T)
     s.close()
+
+
+def test_adapt_remap_with_and_without_capacity(built_lib):
+    """The state remap of a regrid runs in the context's idle buffers while the new mesh fits
+    them, and in buffers of its own when it does not (every leaf splitting: 8x the cells,
+    beyond the 25 % headroom); both give the children their parent's bits."""
+    m = Mesh((2, 2, 2), uniform_leaves((2, 2, 2), 2))
+    rng = np.random.default_rng(3)
+    S = np.empty((5, m.n))
+    S[0] = rng.uniform(0.5, 2.0, m.n)
+    S[1:4] = rng.normal(0, 0.1, (3, m.n))
+    S[4] = rng.uniform(2.0, 3.0, m.n)
+    s = Solver()
+    s.set_mesh(m)
+    s.upload_state(S)
+    x = m.centroids()
+    small = np.where(x[:, 0] < 0.25, 3, 2).astype(np.int32)  # a quarter of the leaves split
+    for split in (small, None):
+        old_level, old_S = s.mesh.level, s.download_state()
+        if split is None:
+            split = (old_level + 1).astype(np.int32)  # every leaf splits
+        new, src = s.adapt(split, with_src=True)
+        assert new.n == old_S.shape[1] + 7 * int((split > old_level).sum())
+        assert np.array_equal(s.download_state(), old_S[:, src])
+    s.close()
