@@ -645,8 +645,8 @@ def train_wall_indicator(kw: dict, dev, amr_cfg: dict, seed: int = 20261203):
     Xs, ys, runs = [], [], 0
     for k in range(TRAIN_RUNS):
         standoff, radius = rng.uniform(1.0, 2.5), rng.uniform(0.05, 0.15)
-        mesh, S0, _ = W.bubble_wall_config3(lmax=TRAIN_LMAX, band_cells=4.0, radius=radius,
-                                            standoff=standoff)
+        mesh, S0, _ = W.bubble_wall_config3(lmax=TRAIN_LMAX, band_cells=WALL_SIZES["config3"][1],
+                                            radius=radius, standoff=standoff)
         s = Solver(device=dev.index, precision=1, **kw)
         s.set_mesh(mesh)
         s.upload_state(S0)
