@@ -71,24 +71,107 @@ struct ffv_mesh;
 int64_t ffv_sibling_group(const ffv_mesh *m, int64_t c);
 
 #ifdef __cplusplus
+#include <unistd.h>
+
 #include <algorithm>
+#include <condition_variable>
+#include <functional>
+#include <mutex>
 #include <thread>
 #include <vector>
 
+inline int host_threads() {
+  return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
+}
+
+// Worker threads kept for the process's lifetime, so that a parallel loop does not pay for
+// starting and joining its threads (~15 us each): a regrid runs dozens of short loops.
+// run(n, fn) calls fn(0) on the calling thread and fn(1..n-1) on workers, and returns once
+// all have finished.  It declines (returns false, the caller then starts threads of its own)
+// when the pool is busy with another caller's loop, when called from inside a loop, when n
+// exceeds its workers, or in a child process forked after the workers started (they do not
+// exist there).  The pool is never destroyed: its threads wait on a condition variable and
+// end with the process.
+class HostPool {
+ public:
+  static HostPool &instance() {
+    static HostPool *p = new HostPool();
+    return *p;
+  }
+  bool run(int n, const std::function<void(int)> &fn) {
+    if (n < 2 || in_loop() || getpid() != pid_ || n - 1 > (int)workers_.size()) return false;
+    std::unique_lock<std::mutex> busy(run_mu_, std::try_to_lock);
+    if (!busy.owns_lock()) return false;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &fn;
+      last_ = n - 1;
+      remaining_ = n - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    in_loop() = true;
+    fn(0);
+    in_loop() = false;
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [&] { return remaining_ == 0; });
+    job_ = nullptr;
+    return true;
+  }
+
+ private:
+  HostPool() : pid_(getpid()) {
+    for (int t = 1; t < host_threads(); t++) workers_.emplace_back([this, t] { loop(t); });
+  }
+  static bool &in_loop() {
+    static thread_local bool f = false;
+    return f;
+  }
+  void loop(int t) {
+    uint64_t seen = 0;
+    for (;;) {
+      const std::function<void(int)> *job;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (t > last_) continue;  // not one of this loop's threads
+        job = job_;
+      }
+      in_loop() = true;
+      (*job)(t);
+      in_loop() = false;
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--remaining_ == 0) done_.notify_one();
+    }
+  }
+  const pid_t pid_;
+  std::vector<std::thread> workers_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)> *job_ = nullptr;
+  int last_ = 0, remaining_ = 0;
+  uint64_t gen_ = 0;
+};
+
 // fn(thread, begin, end) on nthreads contiguous chunks of [0, n), the calling thread taking
-// the first
+// the first.  Loops over at least 2^20 elements run on the pool's workers when it takes them
+// (the pool is created by the first such loop: a process that only ever runs small meshes
+// keeps no idle threads), others on threads started here.
 template <typename Fn>
 inline void parallel_chunks(int64_t n, int nthreads, Fn fn) {
   const int64_t chunk = (n + nthreads - 1) / nthreads;
+  auto part = [&](int t) { fn(t, std::min(n, t * chunk), std::min(n, (t + 1) * chunk)); };
+  if (nthreads < 2) {
+    part(0);
+    return;
+  }
+  if (n >= ((int64_t)1 << 20) && HostPool::instance().run(nthreads, std::function<void(int)>(part)))
+    return;
   std::vector<std::thread> pool;
-  for (int t = 1; t < nthreads; t++)
-    pool.emplace_back([&, t] { fn(t, std::min(n, t * chunk), std::min(n, (t + 1) * chunk)); });
-  fn(0, 0, std::min(n, chunk));
+  for (int t = 1; t < nthreads; t++) pool.emplace_back([&, t] { part(t); });
+  part(0);
   for (auto &th : pool) th.join();
-}
-
-inline int host_threads() {
-  return (int)std::max(1u, std::min(64u, std::thread::hardware_concurrency()));
 }
 #endif
 
