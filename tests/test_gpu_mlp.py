@@ -66,6 +66,21 @@ def test_forward_many_tiles_matches_oracle(built_lib):
     ind.close()
 
 
+@pytest.mark.parametrize("n", [1, 5, 127, 128, 129])
+def test_forward_partial_tile_matches_oracle(n, built_lib):
+    """Fewer rows than one 128-row tile, exactly one, and one more: the rows past n are zero
+    in the tile and never written."""
+    rng = np.random.default_rng(100 + n)
+    ind = Indicator(seed=3)
+    P = random_params(rng)
+    ind.set_params(P)
+    Xf, X, _, _ = data(rng, n)
+    p = ind.forward(X).cpu().numpy()
+    ref, _ = mlp.forward(P.astype(np.float64), Xf)
+    assert p.shape == (n,) and np.abs(p - ref).max() < 2e-3
+    ind.close()
+
+
 def test_predict_equals_forward_of_features(built_lib):
     """ffv_mlp_predict (stencil gather fused with the network) gives the bits of
     ffv_mlp_forward on the rows of ffv_mlp_features."""
