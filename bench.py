@@ -131,9 +131,10 @@ def workload_config(workload: str, n: int | None = None, levels=None) -> dict:
     if workload.startswith("config3"):
         lmax = WALL_SIZES[workload][0]
         size = {"config3": "", "config3m": " (medium size)", "config3s": " (small size)"}[workload]
-        return {"workload": f"config3 bubble collapse near a hyperelastic wall{size}, model 5 "
-                            f"(3 materials), levels 4-{lmax} AMR; FP32-flux + learned AMR against "
-                            "plain FP64 + AMR; MUSCL-HLLC, ghost-fluid, PRELAX 3, RK2",
+        return {"workload": f"config3 bubble collapse near an elastoplastic wall{size} (von Mises "
+                            f"yield 0.3 GPa), model 5 (3 materials), levels 4-{lmax} AMR; FP32-flux "
+                            "+ learned AMR against plain FP64 + AMR; MUSCL-HLLC, ghost-fluid, "
+                            "PRELAX 3, RK2",
                 "cells": n, "levels": levels, "neq": 21,
                 "dt": WALL_CFL * (0.5 / (1 << (lmax - 1))) / C_SOLID, "cfl": WALL_CFL,
                 "cfl_speed": "solid sound speed, finest cell", "parallelism": "single GPU",
@@ -189,7 +190,8 @@ def wl_config1(small: bool = False):
 
 
 def _config3(name: str):
-    """Bubble collapse near a hyperelastic wall, 3 materials (NEQ 21)."""
+    """Bubble collapse near an elastoplastic wall (radial return at the configuration's
+    yield stress), 3 materials (NEQ 21)."""
     from forestfv_public_gb300 import workloads as W
     lmax, band = WALL_SIZES[name]
     mesh, S0, p = W.bubble_wall_config3(lmax=lmax, band_cells=band)
