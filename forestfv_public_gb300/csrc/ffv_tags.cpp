@@ -8,8 +8,11 @@
 #include <stdint.h>
 #include <stdlib.h>
 
+#include <string.h>
+
 #include <algorithm>
 #include <functional>
+#include <memory>
 #include <queue>
 #include <vector>
 
@@ -20,10 +23,19 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   const int64_t n = m->n;
   const int nth = host_threads();
   auto level = [&](int64_t c) { return (int32_t)ffv_info_level(m->info[c]); };
+  // per-leaf byte arrays, filled in parallel (a value-initialised vector fills them, and
+  // takes their first-touch page faults, on one thread)
+  auto bytes = [&](uint8_t v) {
+    std::unique_ptr<uint8_t[]> p(new uint8_t[n > 0 ? n : 1]);
+    uint8_t *q = p.get();
+    parallel_chunks(n, nth, [&](int, int64_t a, int64_t b) { memset(q + a, v, (size_t)(b - a)); });
+    return p;
+  };
   // a leaf's complete group of eight sibling leaves (first leaf, or -1), looked up once and
   // remembered as one byte (0 not looked up, 1 in a complete group, 2 not); each entry is
   // written only by the thread that evaluates its own leaf
-  std::vector<uint8_t> gknown(n, 0);
+  const std::unique_ptr<uint8_t[]> gknown_b = bytes(0);
+  uint8_t *const gknown = gknown_b.get();
   auto group_of = [&](int64_t c) -> int64_t {
     const uint8_t f = gknown[c];
     if (f == 0) {
@@ -81,8 +93,11 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   // passed them too); the next pass's evaluation finds them.  That evaluation visits only
   // "dirty" leaves: all at first, afterwards those one of whose inputs (their own value, a
   // sibling's or a face neighbour's, per rule) changed since they were last evaluated -- a
-  // leaf found unchanged stays unchanged until then.
-  std::vector<uint8_t> queued(n, 0), dirty1(n, 1), dirty2(n, 1);
+  // leaf found unchanged stays unchanged until then.  A sweep with no dirty leaf at all is
+  // skipped (any1 / any2: some leaf of the rule is dirty).
+  const std::unique_ptr<uint8_t[]> queued_b = bytes(0), dirty1_b = bytes(1), dirty2_b = bytes(1);
+  uint8_t *const queued = queued_b.get(), *const dirty1 = dirty1_b.get(), *const dirty2 = dirty2_b.get();
+  bool any1 = true, any2 = true;
   // the readers of split[c]: c itself and, for the coarsening rule, its siblings (which
   // read only whether split[c] is below the level: `flipped`), for the 2:1 rule its face
   // neighbours
@@ -107,8 +122,10 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
       }
     }
   };
-  auto sweep = [&](auto rule, bool sibling_deps, std::vector<uint8_t> &dirty,
-                   std::vector<uint8_t> &dirty_other) -> bool {
+  auto sweep = [&](auto rule, bool sibling_deps, uint8_t *dirty, bool &any, uint8_t *dirty_other,
+                   bool &any_other) -> bool {
+    if (!any) return false;
+    any = false;
     std::vector<std::vector<int64_t>> found(nth);
     parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
       for (int64_t c = a; c < b; c++) {
@@ -143,10 +160,12 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
           }
         } else {
           dirty[d] = 1;
+          any = true;
         }
       });
       // the other rule's readers: at its next sweep
       mark_deps(c, !sibling_deps, flipped, [&](int64_t d) { dirty_other[d] = 1; });
+      any_other = true;
     }
     return true;
   };
@@ -164,9 +183,12 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   };
   // 1 + the pass in which the coarsening rule last changed the leaf, modulo 256 (a stale
   // equal value after 256 passes would only make a leaf dirty that need not be)
-  std::vector<uint8_t> changed_in(n, 0);
+  const std::unique_ptr<uint8_t[]> changed_in_b = bytes(0);
+  uint8_t *const changed_in = changed_in_b.get();
   std::vector<std::vector<int64_t>> chg(nth);  // the leaves each thread's sweep changed
   auto sweep1 = [&](int32_t pass) -> bool {
+    if (!any1) return false;
+    any1 = false;
     parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
       a = align(a);
       b = align(b);
@@ -209,6 +231,8 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
     size_t nchg = 0;
     for (int t = 0; t < nth; t++) nchg += chg[t].size();
     if (nchg == 0) return false;
+    any1 = true;  // the groups that changed were marked dirty again
+    any2 = true;  // and their leaves' face neighbours, below
     // the 2:1 rule's readers of a changed leaf: itself and its face neighbours -- marked
     // from the lists when they are short, else gathered by each reader over all leaves (the
     // face relation is symmetric)
@@ -241,7 +265,7 @@ extern "C" int ffv_tags_smooth(const ffv_mesh *m, int32_t level_max, int32_t *sp
   // would see the same input and change nothing either, so the passes end there.
   for (int32_t pass = 0; pass < level_max + 1; pass++) {
     const bool c1 = sweep1(pass);
-    const bool c2 = sweep(rule2, false, dirty2, dirty1);
+    const bool c2 = sweep(rule2, false, dirty2, any2, dirty1, any1);
     if (!c1 && !c2) break;
   }
   return FFV_OK;
