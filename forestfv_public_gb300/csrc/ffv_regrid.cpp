@@ -17,6 +17,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <memory>
 #include <new>
 #include <vector>
 
@@ -28,14 +29,22 @@ namespace {
 
 constexpr int kDepth = FFV_MAX_LEVEL - 1;  // Morton digits below the tree at the finest level
 
+// The per-leaf arrays are left uninitialised when allocated and written in full by the
+// parallel passes below, which thereby also take their first-touch page faults in parallel
+// (a resized vector would fill them on one thread first).
+template <typename T>
+std::unique_ptr<T[]> uninit(int64_t n) {
+  return std::unique_ptr<T[]>(new (std::nothrow) T[n > 0 ? n : 1]);
+}
+
 struct Leaves {
   int32_t *tij = nullptr, *cij = nullptr;  // new leaves in leaf order (the new mesh's arrays)
-  std::vector<int32_t> lev;
-  int64_t *src = nullptr;        // old leaf copied or split (>= 0), -1 - j merged from j..j+7
-  std::vector<int64_t> own_src;  // src's storage when the caller does not want it
-  std::vector<int32_t> old2new;  // kept old leaves' new index, else -1
-  std::vector<uint8_t> what;     // per old leaf: 0 absorbed, 1 kept, 2 merged parent, 8 split
-  std::vector<int64_t> tsum;     // new leaves before each chunk of old leaves
+  std::unique_ptr<int32_t[]> lev;
+  int64_t *src = nullptr;                // old leaf copied or split (>= 0), -1 - j merged from j..j+7
+  std::unique_ptr<int64_t[]> own_src;    // src's storage when the caller does not want it
+  std::unique_ptr<int32_t[]> old2new;    // kept old leaves' new index, else -1
+  std::unique_ptr<uint8_t[]> what;       // per old leaf: 0 absorbed, 1 kept, 2 merged parent, 8 split
+  std::vector<int64_t> tsum;             // new leaves before each chunk of old leaves
   int64_t nn = 0;
 };
 
@@ -43,7 +52,8 @@ struct Leaves {
 // target is not below its level cannot be part of a merge: no group lookup)
 int count_leaves(const ffv_mesh *m, const int32_t *split, int nth, Leaves &L) {
   const int64_t n = m->n;
-  L.what.resize(n);
+  L.what = uninit<uint8_t>(n);
+  if (!L.what) return FFV_ERR_NOMEM;
   std::vector<int64_t> &tsum = L.tsum;
   tsum.assign(nth + 1, 0);
   std::vector<char> bad(nth, 0);
@@ -71,11 +81,12 @@ int count_leaves(const ffv_mesh *m, const int32_t *split, int nth, Leaves &L) {
 }
 
 // the new leaves written in the order one sweep in leaf order emits them, into L.tij / L.cij
-void fill_leaves(const ffv_mesh *m, int nth, Leaves &L) {
+bool fill_leaves(const ffv_mesh *m, int nth, Leaves &L) {
   const int64_t n = m->n, nn = L.nn;
   const std::vector<int64_t> &tsum = L.tsum;
-  L.lev.resize(nn);
-  L.old2new.resize(n);
+  L.lev = uninit<int32_t>(nn);
+  L.old2new = uninit<int32_t>(n);
+  if (!L.lev || !L.old2new) return false;
   parallel_chunks(n, nth, [&](int t, int64_t a, int64_t b) {
     int64_t o = tsum[t];
     for (int64_t c = a; c < b; c++) {
@@ -112,6 +123,7 @@ void fill_leaves(const ffv_mesh *m, int nth, Leaves &L) {
       }
     }
   });
+  return true;
 }
 
 // rank of each tree in Morton order of its coordinates, by linear index (i * ny + j) * nz + k
@@ -160,10 +172,17 @@ extern "C" int ffv_mesh_adapt(const ffv_mesh *m, const int32_t *split, ffv_mesh 
   if (src) {
     L.src = src;
   } else {
-    L.own_src.resize(nn);
-    L.src = L.own_src.data();
+    L.own_src = uninit<int64_t>(nn);
+    if (!L.own_src) {
+      ffv_mesh_free(nm);
+      return FFV_ERR_NOMEM;
+    }
+    L.src = L.own_src.get();
   }
-  fill_leaves(m, nth, L);
+  if (!fill_leaves(m, nth, L)) {
+    ffv_mesh_free(nm);
+    return FFV_ERR_NOMEM;
+  }
   const int32_t *NT = m->desc.ntrees;
   const std::vector<uint64_t> rank = tree_ranks(NT);
   if (rank.size() >= (1ull << (64 - 3 * kDepth))) {
